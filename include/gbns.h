@@ -1,0 +1,227 @@
+/*
+ * gbns.h -- C ABI of libgbns.so, the GB300 (sm_103a) nested-sampling inner loop.
+ *
+ * All pointers named *_dev are device pointers; the caller owns every buffer (sizes from
+ * gbns_batch_layout).  The library never allocates device memory inside a run, never
+ * synchronises inside gbns_batch_iterate, and reports errors through the return code
+ * (0 = OK, negative = argument/launch error; message from gbns_last_error()).
+ * Per-run device status words (gbns_run_state.status) carry budget/overflow errors.
+ *
+ * Reference interfaces replaced (paths inside the jaxns v2.6.9 source tree, src/jaxns/):
+ *   gbns_batch_init       <- create_init_state            nested_samplers/common/initialisation.py:20-84
+ *                            + create_init_termination_register                   :87-108
+ *   gbns_batch_iterate    <- _main_ns_thread loop body    nested_samplers/sharded/sharded_static.py:487-555
+ *                            (_collect_shell :210-324, get_samples :88-129,
+ *                             UniDimSliceSampler.get_sample samplers/uni_slice_sampler.py:343-441,
+ *                             determine_termination nested_samplers/common/termination.py:13-147)
+ *   gbns_batch_finalize   <- final live-point append      sharded_static.py:833-838
+ *   gbns_batch_results    <- ShardedStaticNestedSampler._to_results  sharded_static.py:652-773
+ *                            (count_crossed_edges internals/tree_structure.py:33-108,
+ *                             compute_evidence_stats internals/shrinkage_statistics.py:131-157)
+ *   gbns_forward          <- Model.forward (vmapped)      framework/model.py:167-176
+ *   gbns_threefry_split   <- jax.random.split under jax_threefry_partitionable
+ *                            (set by internals/mixed_precision.py:11)
+ *   gbns_random_bits64 / gbns_uniform / gbns_normal <- jax.random.bits/uniform/normal (test hooks)
+ *   gbns_count_crossed_edges <- count_crossed_edges       internals/tree_structure.py:33-108
+ *   gbns_evidence_stats   <- compute_evidence_stats       internals/shrinkage_statistics.py:131-157
+ *   gbns_phiw_loglik      <- Model.forward of a linear-Gaussian model, batched over proposals
+ *                            (the user likelihood N(y; Phi w, sigma^2 I); no reference kernel)
+ *   gbns_evidence_adjoint <- jax.grad of EvidenceMaximisation's reweighted log-evidence
+ *                            experimental/evidence_maximisation.py:151-160 (weights :213)
+ */
+#ifndef GBNS_H
+#define GBNS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBNS_VERSION 1
+
+/* likelihood families (a fused CUDA likelihood cannot be an arbitrary Python callable) */
+enum gbns_family {
+    GBNS_LIK_MVN = 0,      /* log N(x; mu, L L^T), L lower Cholesky (params: mu, Linv, c0) */
+    GBNS_LIK_SHELLS = 1,   /* logaddexp of two Gaussian shells (params: c1, c2, R, w)       */
+    GBNS_LIK_LINGAUSS = 2  /* log N(y; Phi w, sigma^2 I) (params: Phi, y, sigma)            */
+};
+
+/* prior quantile per U dimension */
+enum gbns_prior { GBNS_PRIOR_UNIFORM = 0, GBNS_PRIOR_NORMAL = 1 };
+
+/* per-run status bits (gbns_run_state.status) */
+enum gbns_status {
+    GBNS_OK = 0,
+    GBNS_ERR_INIT_BUDGET = 1,    /* init rejection sampling ran out of its evaluation budget */
+    GBNS_ERR_SHRINK_BUDGET = 2,  /* a slice shrink loop ran out of its evaluation budget      */
+    GBNS_ERR_STORE_FULL = 4,     /* iteration budget / store capacity exhausted               */
+    GBNS_ERR_BAD_PARAM = 8
+};
+
+/* TerminationCondition (nested_samplers/common/types.py:26-60); has_* flags mark the
+ * fields that are not None.  max_samples is the already-clamped limit. */
+typedef struct {
+    int has_ess, has_evidence_uncert, has_dlogZ, has_max_samples, has_max_nlik;
+    int has_log_L_contour, has_efficiency, has_rtol, has_atol, has_peak_XL;
+    double ess, evidence_uncert, dlogZ, max_samples, max_nlik;
+    double log_L_contour, efficiency_threshold, rtol, atol, peak_XL_frac;
+} gbns_term_cond;
+
+/* EvidenceCalculation (nested_samplers/common/types.py:12-23), log space, FP64 */
+typedef struct {
+    double log_L, log_X_mean, log_X2_mean, log_Z_mean, log_ZX_mean, log_Z2_mean, log_dZ_mean, log_dZ2_mean;
+} gbns_evcalc;
+
+/* static description of one run */
+typedef struct {
+    int D;            /* U dimensions */
+    int n;            /* live points */
+    int s;            /* shell size (discards per iteration) */
+    int S;            /* num_slices */
+    int K;            /* phantoms saved per chain (num_phantom_save) */
+    int family;       /* gbns_family */
+    int midpoint;     /* midpoint_shrink */
+    int uniform_phase;/* 1: run the UniformSampler phase first (init_efficiency_threshold > 0) */
+    int N;            /* rows of Phi (linear-Gaussian family) */
+    int pad0;
+    double init_efficiency_threshold;
+    long long cap;         /* store capacity (max_samples, rounded) */
+    long long live_off;    /* index of the run's first live point */
+    long long store_off;   /* index of the run's first store slot */
+    long long shell_off;   /* index of the run's first shell output */
+    long long param_off;   /* index of the run's first float parameter */
+    long long prior_off;   /* index of the run's first prior-table entry */
+    long long ustore_off;  /* float offset of the run's U store, or -1 when U is not stored */
+    long long liveU_off;   /* float offset of the run's live U block ([n, D]) */
+    long long newU_off;    /* float offset of the run's shell-output U block ([s, D]) */
+    long long phU_off;     /* float offset of the run's phantom U block ([s, K, D]) */
+    long long phL_off;     /* index of the run's first phantom log L ([s, K]) */
+    gbns_term_cond tc;
+} gbns_run_desc;
+
+/* TerminationRegister (types.py:127-138) + NestedSamplerState scalars (types.py:141-145) */
+typedef struct {
+    gbns_evcalc ev;
+    gbns_evcalc ev_rem;
+    double log_L_contour;
+    double efficiency;
+    double relative_spread;
+    double absolute_spread;
+    double peak_log_XL;
+    long long num_likelihood_evaluations;
+    long long num_samples;      /* NestedSamplerState.num_samples */
+    long long next_sample_idx;  /* NestedSamplerState.next_sample_idx */
+    long long iterations;
+    uint32_t key[2];            /* NestedSamplerState.key */
+    int plateau;
+    int no_seed_points;
+    int phase;                  /* 0: uniform phase, 1: slice phase, 2: finished */
+    int done;                   /* termination decided for the current phase */
+    int termination_reason;
+    int parity;                 /* which live buffer is current */
+    int status;                 /* gbns_status bits */
+    int pad1;
+} gbns_run_state;
+
+/* device buffers of a batch of runs (all *_dev, caller-allocated) */
+typedef struct {
+    int num_runs;
+    int nmax;                       /* largest n over runs (<= 4096) */
+    int ncoef_n;                    /* largest count covered by the ncoef table */
+    const gbns_run_desc *runs;      /* [R] */
+    gbns_run_state *state;          /* [R] */
+    float *live_U[2];               /* [sum n*D] */
+    float *live_L[2];               /* [sum n] */
+    float *live_Lc[2];              /* [sum n] */
+    int *live_E[2];                 /* [sum n] likelihood evaluations */
+    int *live_S[2];                 /* [sum n] sender node */
+    float *new_U;                   /* [sum s*D] */
+    float *new_L;                   /* [sum s] */
+    int *new_E;                     /* [sum s] */
+    float *ph_U;                    /* [sum s*K*D] */
+    float *ph_L;                    /* [sum s*K] */
+    float *store_L;                 /* [sum cap] */
+    int *store_S;                   /* [sum cap] */
+    int *store_E;                   /* [sum cap] */
+    uint8_t *store_P;               /* [sum cap] phantom flag */
+    float *store_U;                 /* [sum cap*D] or NULL */
+    const float *fparams;           /* family parameters */
+    const int *prior_kind;          /* [sum D] */
+    const float *prior_a;           /* [sum D] */
+    const float *prior_b;           /* [sum D] */
+    const double *ncoef;            /* [(ncoef_n+1) * 8] FP64 shrinkage coefficients per count */
+    const int *items;               /* [num_items * 4] (run, chain_begin, chain_count, 0) */
+    int num_items;
+    int bucket_begin[8];            /* work-item ranges per dimension bucket */
+    int bucket_end[8];
+    int chains_per_item;
+    int max_evals_per_slice;        /* shrink-loop evaluation budget per slice */
+} gbns_batch;
+
+/* results buffers (device) */
+typedef struct {
+    int *samples_indices;           /* [sum cap] */
+    int *num_live_points;           /* [sum cap] */
+    float *log_L_samples;           /* [sum cap] sorted */
+    double *log_dp_mean;            /* [sum cap] */
+    double *log_X_mean;             /* [sum cap] */
+    int *nevals_sorted;             /* [sum cap] */
+    float *U_sorted;                /* [sum cap*D] or NULL */
+    double *scalars;                /* [R * 8]: log_Z_mean, log_Z_uncert, ESS, H_mean,
+                                       total_num_samples, total_phantom, total_nevals, log_efficiency */
+    long long *scratch_ll;          /* [2 * (sum cap + R)] sort scratch */
+    int *scratch_i;                 /* [sum cap + R] degree scratch */
+} gbns_results_bufs;
+
+int gbns_version(void);
+const char *gbns_last_error(void);
+/* sizeof of gbns_term_cond, gbns_evcalc, gbns_run_desc, gbns_run_state, gbns_batch,
+ * gbns_results_bufs (binding self-check; no reference counterpart) */
+int gbns_abi_sizes(long long *out, int n);
+
+/* RNG test hooks (device pointers): key is [2] uint32 */
+int gbns_threefry2x32(const uint32_t *key_dev, const uint32_t *counts_dev, uint32_t *out_dev, long long n,
+                      void *stream);
+int gbns_threefry_split(const uint32_t *key_dev, uint32_t *out_dev, long long n, void *stream);
+int gbns_random_bits64(const uint32_t *key_dev, uint64_t *out_dev, long long n, void *stream);
+int gbns_uniform(const uint32_t *key_dev, float *out_dev, long long n, void *stream);
+int gbns_normal(const uint32_t *key_dev, float *out_dev, long long n, void *stream);
+
+/* Model.forward over B points of one run's model: U [B, D] -> log L [B] */
+int gbns_forward(const gbns_batch *batch, int run, const float *U_dev, float *logL_dev, long long B,
+                 void *stream);
+
+/* NS batch: init, K iterations (graph-capturable), finalize, results */
+int gbns_batch_init(const gbns_batch *batch, void *stream);
+int gbns_batch_iterate(const gbns_batch *batch, int num_iterations, void *stream);
+int gbns_batch_finalize(const gbns_batch *batch, void *stream);
+/* the two halves of one iteration (gbns_batch_iterate = shell + merge), so a caller can
+ * time the slice sampler separately:
+ *   gbns_batch_shell <- get_samples / UniDimSliceSampler.get_sample for every active run
+ *                       (sharded_static.py:88-129, uni_slice_sampler.py:343-441)
+ *   gbns_batch_merge <- the rest of _collect_shell + the while-loop condition
+ *                       (sharded_static.py:240-323, :480-485, :833-838) */
+int gbns_batch_shell(const gbns_batch *batch, void *stream);
+/* record a CUDA event on a stream; inside stream capture it becomes an event-record node of
+ * the graph, so kernel time can be read back after each replay (timing plumbing; no
+ * reference counterpart) */
+int gbns_record_event(void *event, void *stream);
+int gbns_batch_merge(const gbns_batch *batch, void *stream);
+int gbns_batch_results(const gbns_batch *batch, const gbns_results_bufs *res, void *stream);
+
+/* One shell of the slice sampler for every run (test hook: no merge, no register) */
+int gbns_slice_shell(const gbns_batch *batch, const float *Lstar_dev, const uint32_t *keys_dev, void *stream);
+
+/* Standalone tree count and evidence statistics for one sample set (device pointers) */
+int gbns_count_crossed_edges(const int *sender_dev, const float *log_L_dev, long long N, int *samples_indices_dev,
+                             int *num_live_points_dev, long long *scratch_ll_dev, int *scratch_i_dev, void *stream);
+int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,
+                        int nmax, gbns_evcalc *final_dev, double *log_X_mean_dev, double *log_dZ_mean_dev,
+                        double *log_Z_mean_dev, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

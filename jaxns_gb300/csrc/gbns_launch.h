@@ -1,0 +1,21 @@
+// gbns_launch.h -- host-side launchers shared between the translation units of libgbns.so.
+#pragma once
+#include <cuda_runtime.h>
+#include "../../include/gbns.h"
+
+namespace gbns {
+
+cudaError_t launch_slice_shells(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
+cudaError_t launch_init(const gbns_batch &b, long long total_points, cudaStream_t stream);
+cudaError_t launch_merge(const gbns_batch &b, cudaStream_t stream);
+cudaError_t launch_finalize(const gbns_batch &b, cudaStream_t stream);
+cudaError_t launch_forward(const gbns_batch &b, int run, const float *U, float *logL, long long B, cudaStream_t stream);
+cudaError_t launch_results(const gbns_batch &b, const gbns_results_bufs &res, cudaStream_t stream);
+cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long long N, int *samples_indices,
+                                       int *num_live, long long *scratch_ll, int *scratch_i, cudaStream_t stream);
+cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
+                                  gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream);
+cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n,
+                       cudaStream_t stream);
+
+}  // namespace gbns

@@ -1,0 +1,298 @@
+// gbns_results.cu -- sample-tree live-point counting, FP64 evidence statistics and the
+// NestedSamplerResults scalars (ShardedStaticNestedSampler._to_results,
+// nested_samplers/sharded/sharded_static.py:652-773), plus the RNG test hooks.
+//
+// count_crossed_edges (internals/tree_structure.py:33-108) needs a stable argsort of the
+// N+1 node log-likelihoods.  Dead points are appended in non-decreasing order except for
+// phantoms and rejection-sampler caps, so the CTA first tests sortedness and only runs the
+// LSD radix sort (4 x 8-bit digits, stable by construction) when it is needed.
+#include "gbns_device.cuh"
+#include "gbns_launch.h"
+
+namespace gbns {
+
+__device__ __forceinline__ unsigned long long node_key(const float *L, long long i) {
+  // node 0 is the root at -inf; node i+1 is sample i
+  const float v = i == 0 ? -INFINITY : L[i - 1];
+  return ((unsigned long long)ordered_key(v) << 32) | (unsigned long long)(unsigned)i;
+}
+
+struct RadixSmem {
+  int wcount[32][257];
+  int base[256];
+  int tile_count[256];
+  int hist[4][256];
+  int flag;
+  long long carry;
+};
+
+// Stable ascending sort of the N+1 node keys (by their upper 32 bits).  Result in a (perm
+// in the low 32 bits).  a, tmp: [N+1] scratch.  blockDim.x must be 1024.
+__device__ unsigned long long *cta_sort_nodes(const float *L, long long N, unsigned long long *a,
+                                              unsigned long long *tmp, RadixSmem &sm) {
+  const long long M = N + 1;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) sm.flag = 1;
+  for (int q = tid; q < 4 * 256; q += blockDim.x) (&sm.hist[0][0])[q] = 0;
+  __syncthreads();
+  int sorted = 1;
+  for (long long i = tid; i < M; i += blockDim.x) {
+    const unsigned long long k = node_key(L, i);
+    a[i] = k;
+    if (i > 0 && (node_key(L, i - 1) >> 32) > (k >> 32)) sorted = 0;
+    const uint32_t key = (uint32_t)(k >> 32);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) atomicAdd(&sm.hist[d][(key >> (8 * d)) & 255], 1);
+  }
+  if (!sorted) sm.flag = 0;
+  __syncthreads();
+  if (sm.flag) return a;
+  unsigned long long *src = a, *dst = tmp;
+  for (int d = 0; d < 4; ++d) {
+    // exclusive prefix of the digit histogram
+    if (tid == 0) {
+      int acc = 0;
+      for (int q = 0; q < 256; ++q) {
+        sm.base[q] = acc;
+        acc += sm.hist[d][q];
+      }
+    }
+    for (int q = tid; q < 32 * 257; q += blockDim.x) (&sm.wcount[0][0])[q] = 0;
+    __syncthreads();
+    for (long long t0 = 0; t0 < M; t0 += blockDim.x) {
+      const long long i = t0 + tid;
+      const bool valid = i < M;
+      const unsigned long long k = valid ? src[i] : 0ull;
+      const int dig = valid ? (int)(((uint32_t)(k >> 32) >> (8 * d)) & 255) : 256;
+      const unsigned peers = __match_any_sync(0xffffffffu, dig);
+      const int rank = __popc(peers & ((1u << lane) - 1u));
+      if (valid && rank == 0) sm.wcount[warp][dig] = __popc(peers);
+      __syncthreads();
+      if (tid < 256) {
+        int run = 0;
+        for (int w = 0; w < 32; ++w) {
+          const int c = sm.wcount[w][tid];
+          sm.wcount[w][tid] = run;
+          run += c;
+        }
+        sm.tile_count[tid] = run;
+      }
+      __syncthreads();
+      if (valid) dst[sm.base[dig] + sm.wcount[warp][dig] + rank] = k;
+      __syncthreads();
+      if (tid < 256) {
+        sm.base[tid] += sm.tile_count[tid];
+        for (int w = 0; w < 32; ++w) sm.wcount[w][tid] = 0;
+      }
+      __syncthreads();
+    }
+    unsigned long long *t = src;
+    src = dst;
+    dst = t;
+  }
+  return src;
+}
+
+// count_crossed_edges on one sample set (static variant).  perm: sorted node keys.
+// deg: [N+1] scratch.  Outputs [N].
+__device__ void cta_count_edges(const int *sender, long long N, const unsigned long long *perm, int *deg,
+                                int *samples_indices, int *num_live, RadixSmem &sm) {
+  const long long M = N + 1;
+  for (long long i = threadIdx.x; i < M; i += blockDim.x) deg[i] = 0;
+  __syncthreads();
+  for (long long i = threadIdx.x; i < N; i += blockDim.x) atomicAdd(&deg[max(sender[i], 0)], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) sm.carry = 1;
+  __syncthreads();
+  __shared__ long long wsum[32];
+  for (long long t0 = 0; t0 < M; t0 += blockDim.x) {
+    const long long i = t0 + threadIdx.x;
+    const int node = i < M ? (int)(perm[i] & 0xffffffffu) : 0;
+    long long v = i < M ? (long long)deg[node] - 1 : 0;
+    v = warp_incl_scan(v);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      long long x = wsum[lane];
+      x = warp_incl_scan(x);
+      wsum[lane] = x;
+    }
+    __syncthreads();
+    const long long crossed = sm.carry + v + (w > 0 ? wsum[w - 1] : 0);
+    if (i < N) {
+      num_live[i] = (int)crossed;
+    }
+    if (i >= 1 && i < M) samples_indices[i - 1] = node - 1;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) sm.carry = crossed;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const float *L, long long N,
+                                                      int *samples_indices, int *num_live,
+                                                      unsigned long long *scratch, int *deg) {
+  __shared__ RadixSmem sm;
+  unsigned long long *perm = cta_sort_nodes(L, N, scratch, scratch + (N + 1), sm);
+  cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm);
+}
+
+__global__ void k_evidence_stats(const float *L, const int *nl, long long N, const double *ncoef, int nmax,
+                                 gbns_evcalc *fin, double *lX, double *ldZ, double *lZ) {
+  gbns_evcalc e;
+  e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
+  e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
+  EvAcc acc = evacc_from(e);
+  evidence_scan_warp(acc, L, N, 0, 0, nl, ncoef, nmax, lX, ldZ, lZ);
+  if (threadIdx.x == 0) *fin = evacc_to(acc, N > 0 ? (double)L[N - 1] : -INFINITY);
+}
+
+// ------------------------------------------------------------ results ----
+
+__global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_bufs res) {
+  __shared__ RadixSmem sm;
+  __shared__ double dred[32];
+  __shared__ long long lred[32];
+  __shared__ double s_lz[4];
+  const int r = blockIdx.x;
+  const gbns_run_desc &rd = b.runs[r];
+  const gbns_run_state &st = b.state[r];
+  const long long N = st.num_samples < rd.cap ? st.num_samples : rd.cap;
+  const long long so = rd.store_off;
+  const int D = rd.D;
+  unsigned long long *scratch = (unsigned long long *)res.scratch_ll + 2 * (so + r);
+  int *deg = res.scratch_i + (so + r);
+  int *si = res.samples_indices + so;
+  int *nl = res.num_live_points + so;
+  const unsigned long long *perm = cta_sort_nodes(b.store_L + so, N, scratch, scratch + (N + 1), sm);
+  cta_count_edges(b.store_S + so, N, perm, deg, si, nl, sm);
+  __syncthreads();
+  // gather in sorted order
+  float *Ls = res.log_L_samples + so;
+  int *Es = res.nevals_sorted + so;
+  long long ev_sum = 0, ph_sum = 0;
+  for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+    const int k = si[i];
+    Ls[i] = b.store_L[so + k];
+    const int e = b.store_E[so + k];
+    Es[i] = e;
+    ev_sum += e;
+    ph_sum += b.store_P[so + i];
+  }
+  if (res.U_sorted && rd.ustore_off >= 0 && b.store_U) {
+    float *Us = res.U_sorted + rd.ustore_off;
+    const float *Ust = b.store_U + rd.ustore_off;
+    for (long long q = threadIdx.x; q < N * D; q += blockDim.x) {
+      const long long i = q / D, j = q % D;
+      Us[q] = Ust[(long long)si[i] * D + j];
+    }
+  }
+  const long long total_evals = cta_sum_ll(ev_sum, lred);
+  const long long total_phantom = cta_sum_ll(ph_sum, lred);
+  __syncthreads();
+  // evidence statistics (warp 0)
+  double *lX = res.log_X_mean + so, *ldp = res.log_dp_mean + so;
+  if (threadIdx.x < 32) {
+    gbns_evcalc e;
+    e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
+    e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
+    EvAcc acc = evacc_from(e);
+    evidence_scan_warp(acc, Ls, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr);
+    if (threadIdx.x == 0) {
+      const gbns_evcalc f = evacc_to(acc, 0.0);
+      s_lz[0] = f.log_Z_mean;
+      s_lz[1] = f.log_Z2_mean;
+      s_lz[2] = f.log_dZ2_mean;
+    }
+  }
+  __syncthreads();
+  // normalise_log_space(log_dZ_mean) and H (sharded_static.py:726-737)
+  float mx = -INFINITY;
+  for (long long i = threadIdx.x; i < N; i += blockDim.x) mx = fmaxf(mx, (float)ldp[i]);
+  mx = cta_max_f(mx, (float *)dred);
+  double se = 0.0;
+  if (mx > -INFINITY)
+    for (long long i = threadIdx.x; i < N; i += blockDim.x) se += (double)__expf((float)(ldp[i] - (double)mx));
+  se = cta_sum_d(se, dred);
+  const double norm = (mx > -INFINITY) ? (double)mx + log(se) : -INFINITY;
+  const double lZ = s_lz[0], lZ2 = s_lz[1], ldZ2 = s_lz[2];
+  const double mu = 2.0 * lZ - 0.5 * lZ2;
+  double h1 = 0.0, h2 = 0.0;
+  for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+    const double v = (norm > -INFINITY) ? ldp[i] - norm : -INFINITY;
+    ldp[i] = v;
+    const double w = (v > -INFINITY) ? (double)__expf((float)v) : 0.0;
+    h1 += w * ((v > -INFINITY) ? (double)Ls[i] : 0.0);
+    h2 += w * (-lX[i]);
+  }
+  h1 = cta_sum_d(h1, dred);
+  h2 = cta_sum_d(h2, dred);
+  if (threadIdx.x == 0) {
+    double var = lZ2 - 2.0 * lZ;
+    var = (var != var) ? var : fmax(var, 2.220446049250313e-16);
+    const double pf = (double)total_phantom / (double)N;
+    const double k = pf / (1.0 - pf);
+    double *sc = res.scalars + 8 * (size_t)r;
+    sc[0] = mu;
+    sc[1] = sqrt(var) * sqrt(1.0 + k);
+    sc[2] = exp(2.0 * lZ - ldZ2) / (1.0 + k);
+    const double H_inst = -(h1 - mu);
+    sc[3] = isfinite(H_inst) ? H_inst : -h2;
+    sc[4] = (double)N;
+    sc[5] = (double)total_phantom;
+    sc[6] = (double)total_evals;
+    sc[7] = log((double)N) - log((double)total_evals);
+  }
+}
+
+// ---------------------------------------------------------- RNG hooks ----
+
+__global__ void k_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const Key k = {key[0], key[1]};
+  if (mode == 0) {  // raw threefry2x32 of (counts[2i], counts[2i+1])
+    uint32_t a, c;
+    threefry2x32(k.k0, k.k1, counts[2 * i], counts[2 * i + 1], a, c);
+    ((uint32_t *)out)[2 * i] = a;
+    ((uint32_t *)out)[2 * i + 1] = c;
+  } else if (mode == 1) {  // split
+    const Key s = fold(k, (uint32_t)i);
+    ((uint32_t *)out)[2 * i] = s.k0;
+    ((uint32_t *)out)[2 * i + 1] = s.k1;
+  } else if (mode == 2) {
+    ((uint64_t *)out)[i] = bits64(k, (uint32_t)i);
+  } else if (mode == 3) {
+    ((float *)out)[i] = uniform01(bits64(k, (uint32_t)i));
+  } else {
+    ((float *)out)[i] = normal_from_bits(bits64(k, (uint32_t)i));
+  }
+}
+
+cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n,
+                       cudaStream_t stream) {
+  if (n <= 0) return cudaSuccess;
+  k_rng<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(mode, key, counts, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_results(const gbns_batch &b, const gbns_results_bufs &res, cudaStream_t stream) {
+  k_results<<<b.num_runs, 1024, 0, stream>>>(b, res);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long long N, int *samples_indices,
+                                       int *num_live, long long *scratch_ll, int *scratch_i, cudaStream_t stream) {
+  k_count_edges<<<1, 1024, 0, stream>>>(sender, L, N, samples_indices, num_live, (unsigned long long *)scratch_ll,
+                                        scratch_i);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
+                                  gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream) {
+  k_evidence_stats<<<1, 32, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
+  return cudaGetLastError();
+}
+
+}  // namespace gbns

@@ -1,0 +1,283 @@
+// gbns_slice.cu -- the fused uni-dimensional slice sampler for one shell of every run.
+//
+// One thread owns one Markov chain (UniDimSliceSampler.get_sample,
+// samplers/uni_slice_sampler.py:343-441, via BaseAbstractMarkovSampler._get_sample,
+// samplers/bases.py:63-75).  The chain's slice loop and the shrink while-loop of
+// _new_proposal (uni_slice_sampler.py:114-273) are flattened into one loop in which every
+// iteration makes exactly one likelihood evaluation, so the threads of a warp stay in step
+// whatever their shrink counts.  The U->X prior quantile and the likelihood are evaluated
+// in registers; the run's parameters (mu, Linv, prior tables) sit in shared memory and
+// are read as broadcasts because every thread of a CTA works on chains of the same run.
+#include "gbns_device.cuh"
+#include "gbns_launch.h"
+
+namespace gbns {
+
+template <int DMAX, int FAM>
+struct RunSmem {
+  float a[DMAX], b[DMAX];
+  int kind[DMAX];
+  float p0[DMAX];                       // MVN: mu      SHELLS: c1
+  float p1[FAM == GBNS_LIK_MVN ? DMAX * DMAX : DMAX];  // MVN: Linv   SHELLS: c2
+  float c0, R, w, norm;
+  int m;                                // live points above the contour
+};
+
+template <int DMAX, int FAM>
+__device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, const float *u0, const float *d, float t) {
+  float x[DMAX];
+#pragma unroll
+  for (int j = 0; j < DMAX; ++j) {
+    if (j < D) {
+      const float u = fmaf(t, d[j], u0[j]);
+      x[j] = prior_quantile(P.kind[j], P.a[j], P.b[j], u);
+    }
+  }
+  float v;
+  if (FAM == GBNS_LIK_MVN) {
+    float s = 0.0f;
+#pragma unroll
+    for (int j = 0; j < DMAX; ++j)
+      if (j < D) x[j] -= P.p0[j];
+#pragma unroll
+    for (int i = 0; i < DMAX; ++i) {
+      if (i < D) {
+        float acc = 0.0f;
+#pragma unroll
+        for (int j = 0; j <= i; ++j) acc = fmaf(P.p1[i * DMAX + j], x[j], acc);
+        s = fmaf(acc, acc, s);
+      }
+    }
+    v = fmaf(-0.5f, s, P.c0);
+  } else {
+    float r1 = 0.0f, r2 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < DMAX; ++j) {
+      if (j < D) {
+        const float e1 = x[j] - P.p0[j], e2 = x[j] - P.p1[j];
+        r1 = fmaf(e1, e1, r1);
+        r2 = fmaf(e2, e2, r2);
+      }
+    }
+    const float z1 = (sqrtf(r1) - P.R) / P.w, z2 = (sqrtf(r2) - P.R) / P.w;
+    const float s1 = fmaf(-0.5f * z1, z1, -P.norm), s2 = fmaf(-0.5f * z2, z2, -P.norm);
+    const float m = fmaxf(s1, s2), dd = s1 - s2;
+    v = (dd != dd) ? s1 + s2 : m + log1pf(__expf(-fabsf(dd)));
+  }
+  return (v != v) ? -INFINITY : v;  // NaN -> -inf (framework/ops.py:323-325)
+}
+
+template <int DMAX>
+__device__ __forceinline__ void sample_direction(Key k, int D, float *d) {
+  if (D == 1) { d[0] = 1.0f; return; }
+  float s = 0.0f;
+#pragma unroll
+  for (int j = 0; j < DMAX; ++j) {
+    if (j < D) {
+      d[j] = normal_from_bits(bits64(k, (uint32_t)j));
+      s = fmaf(d[j], d[j], s);
+    }
+  }
+  const float nrm = sqrtf(s);
+#pragma unroll
+  for (int j = 0; j < DMAX; ++j)
+    if (j < D) d[j] = d[j] / nrm;
+}
+
+// linspace(0.5, 1, S)[j] as jnp.linspace evaluates it
+__device__ __forceinline__ float slice_alpha(int j, int S) {
+  if (S == 1) return 0.5f;
+  if (j == S - 1) return 1.0f;
+  const float step = (float)j / (float)(S - 1);
+  return 0.5f * (1.0f - step) + step;
+}
+
+template <int DMAX, int FAM>
+__global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begin, const float *__restrict__ Lstar_in,
+                                                      const uint32_t *__restrict__ keys_in) {
+  __shared__ RunSmem<DMAX, FAM> P;
+  const int *it = b.items + 4 * (size_t)(item_begin + blockIdx.x);
+  const int r = it[0], c_begin = it[1], c_count = it[2];
+  const gbns_run_desc &rd = b.runs[r];
+  gbns_run_state &st = b.state[r];
+  if (!keys_in && (st.done || st.phase != 1)) return;
+  const int D = rd.D, n = rd.n, S = rd.S, K = rd.K;
+  const int par = st.parity;
+  const float *__restrict__ liveL = b.live_L[par] + rd.live_off;
+  const float *__restrict__ liveU = b.live_U[par] + rd.liveU_off;
+
+  // --- stage the run's parameters
+  const float *fp = b.fparams + rd.param_off;
+  for (int j = threadIdx.x; j < DMAX; j += blockDim.x) {
+    const bool ok = j < D;
+    P.a[j] = ok ? b.prior_a[rd.prior_off + j] : 0.0f;
+    P.b[j] = ok ? b.prior_b[rd.prior_off + j] : 0.0f;
+    P.kind[j] = ok ? b.prior_kind[rd.prior_off + j] : 0;
+    P.p0[j] = ok ? fp[j] : 0.0f;
+    if (FAM == GBNS_LIK_SHELLS) P.p1[j] = ok ? fp[D + j] : 0.0f;
+  }
+  if (FAM == GBNS_LIK_MVN) {
+    for (int q = threadIdx.x; q < DMAX * DMAX; q += blockDim.x) {
+      const int i = q / DMAX, j = q % DMAX;
+      P.p1[q] = (i < D && j <= i) ? fp[D + i * D + j] : 0.0f;
+    }
+  }
+  const float Lstar = Lstar_in ? Lstar_in[r] : liveL[rd.s - 1];
+  if (threadIdx.x == 0) {
+    if (FAM == GBNS_LIK_MVN) {
+      P.c0 = fp[D + D * D];
+    } else {
+      P.R = fp[2 * D];
+      P.w = fp[2 * D + 1];
+      P.norm = fp[2 * D + 2];
+    }
+    // m = #live points with log L > L* (the live set is sorted ascending)
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (liveL[mid] > Lstar) hi = mid; else lo = mid + 1;
+    }
+    P.m = n - lo;
+  }
+  __syncthreads();
+
+  const int c = c_begin + threadIdx.x;
+  if (threadIdx.x >= c_count) return;
+
+  // --- keys: _collect_shell split (sharded_static.py:248) then split(sample_key, s)[c]
+  Key sample_key;
+  if (keys_in) {
+    sample_key.k0 = keys_in[2 * r];
+    sample_key.k1 = keys_in[2 * r + 1];
+  } else {
+    const Key k0 = {st.key[0], st.key[1]};
+    sample_key = fold(fold(k0, 0u), 1u);
+  }
+  const Key kc = fold(sample_key, (uint32_t)c);
+  const Key chain_key = fold(kc, 0u), seed_key = fold(kc, 1u);
+
+  // --- seed point: resample_indicies over the mask log L > L* (internals/random.py:34-84)
+  const int m = P.m;
+  int idx = 0;
+  if (m > 0) {
+    const uint64_t M52 = bits64(seed_key, 0u) >> 12;
+    const uint64_t q = (1ull << 52) - M52;  // (1 - U) * 2^52
+    const uint64_t lo = (uint64_t)m * q, hi = __umul64hi((uint64_t)m, q);
+    uint64_t kk = (hi << 12) | (lo >> 52);
+    if (lo & ((1ull << 52) - 1)) kk += 1;  // ceil(m (1 - U))
+    idx = (n - m) + (int)kk - 1;
+  }
+  float u0[DMAX], d[DMAX];
+#pragma unroll
+  for (int j = 0; j < DMAX; ++j) u0[j] = (j < D) ? liveU[(size_t)idx * D + j] : 0.0f;
+  float logL0 = liveL[idx];
+
+  const Key direction_key = fold(chain_key, 0u), slices_key = fold(chain_key, 1u);
+  sample_direction<DMAX>(direction_key, D, d);
+
+  // --- flattened slice / shrink loop
+  int j = 0;
+  bool start = true;
+  float left = 0.f, right = 0.f, t = 0.f, alpha = 0.5f;
+  Key ck = {0u, 0u}, after_key = {0u, 0u};
+  int total = 0, in_slice = 0;
+  const int budget = b.max_evals_per_slice;
+  const size_t out = (size_t)rd.shell_off + c;
+  float *phU = b.ph_U + rd.phU_off + (size_t)c * K * D;
+  float *phL = b.ph_L + rd.phL_off + (size_t)c * K;
+  bool failed = false;
+  while (j < S) {
+    float u;
+    if (start) {
+      const Key kj = fold(slices_key, (uint32_t)j);
+      ck = fold(kj, 0u);
+      const Key t_key = fold(kj, 2u);
+      after_key = fold(kj, 3u);
+      alpha = slice_alpha(j, S);
+      // _slice_bounds (uni_slice_sampler.py:41-64)
+      float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
+#pragma unroll
+      for (int q = 0; q < DMAX; ++q) {
+        if (q < D) {
+          const float t1 = (1.0f - u0[q]) / d[q];
+          const float t0 = -u0[q] / d[q];
+          t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
+          t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
+          t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
+          t0l = fmaxf(t0l, t0 <= 0.f ? t0 : -INFINITY);
+        }
+      }
+      right = fminf(t0r, t1r);
+      left = fmaxf(t0l, t1l);
+      u = uniform01(bits64(t_key, 0u));
+      in_slice = 0;
+    } else {
+      const Key nk = fold(ck, 0u), tk = fold(ck, 1u);
+      // _shrink_interval (uni_slice_sampler.py:92-111)
+      if (t < 0.f) left = t;
+      if (t > 0.f) right = t;
+      if (rd.midpoint) {
+        if (t < 0.f) left = alpha * left;
+        if (t > 0.f) right = alpha * right;
+      }
+      u = uniform01(bits64(tk, 0u));
+      ck = nk;
+    }
+    // _pick_point_in_interval (uni_slice_sampler.py:67-89)
+    t = fmaf(u, right - left, left);
+    const float logL = loglik<DMAX, FAM>(P, D, u0, d, t);
+    ++total;
+    ++in_slice;
+    const bool accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
+    if (accept || in_slice >= budget) {
+      if (!accept) failed = true;
+#pragma unroll
+      for (int q = 0; q < DMAX; ++q)
+        if (q < D) u0[q] = fmaf(t, d[q], u0[q]);
+      logL0 = logL;
+      const int p = j - (S - 1 - K);
+      if (K > 0 && p >= 0 && j < S - 1) {
+        for (int q = 0; q < D; ++q) phU[(size_t)p * D + q] = u0[q];
+        phL[p] = logL;
+      }
+      ++j;
+      start = true;
+      if (j < S) sample_direction<DMAX>(after_key, D, d);
+    } else {
+      start = false;
+    }
+  }
+  float *nu = b.new_U + rd.newU_off + (size_t)c * D;
+  for (int q = 0; q < D; ++q) nu[q] = u0[q];
+  b.new_L[out] = logL0;
+  b.new_E[out] = total;
+  if (failed) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
+}
+
+template <int DMAX>
+static cudaError_t launch_bucket(const gbns_batch &b, int fam, int ib, int ie, const float *Lstar, const uint32_t *keys,
+                                 cudaStream_t stream) {
+  const int nblk = ie - ib;
+  if (nblk <= 0) return cudaSuccess;
+  const int threads = b.chains_per_item;
+  if (fam == GBNS_LIK_MVN)
+    k_slice_shell<DMAX, GBNS_LIK_MVN><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+  else
+    k_slice_shell<DMAX, GBNS_LIK_SHELLS><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+  return cudaGetLastError();
+}
+
+// Buckets are (family, DMAX) pairs: bucket = fam * 4 + {0: D<=8, 1: D<=16, 2: D<=32, 3: D<=64}.
+cudaError_t launch_slice_shells(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream) {
+  for (int fam = 0; fam < 2; ++fam) {
+    cudaError_t e;
+    const int o = fam * 4;
+    if ((e = launch_bucket<8>(b, fam, b.bucket_begin[o + 0], b.bucket_end[o + 0], Lstar, keys, stream))) return e;
+    if ((e = launch_bucket<16>(b, fam, b.bucket_begin[o + 1], b.bucket_end[o + 1], Lstar, keys, stream))) return e;
+    if ((e = launch_bucket<32>(b, fam, b.bucket_begin[o + 2], b.bucket_end[o + 2], Lstar, keys, stream))) return e;
+    if ((e = launch_bucket<64>(b, fam, b.bucket_begin[o + 3], b.bucket_end[o + 3], Lstar, keys, stream))) return e;
+  }
+  return cudaSuccess;
+}
+
+}  // namespace gbns

@@ -1,0 +1,467 @@
+"""Batched nested-sampling engine: device buffers of many independent runs and the
+iteration driver over libgbns.so.
+
+One ``NSBatch`` holds R runs (uneven D, n, store size) in packed structure-of-arrays
+buffers.  ``run()`` initialises the live points, then replays a captured CUDA graph of
+``block`` iterations (each iteration = one slice-sampler shell for every active run + one
+merge/register/termination kernel) until every run has terminated, and finally computes
+the results (tree live-point counts, FP64 evidence statistics) on the device.
+
+Reference correspondence (jaxns v2.6.9, src/jaxns/):
+  ShardedStaticNestedSampler._run      nested_samplers/sharded/sharded_static.py:775-851
+  _main_ns_thread / _collect_shell     sharded_static.py:427-574 / :210-324
+  _to_results                          sharded_static.py:652-773
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional
+
+import numpy as np
+import torch
+
+from . import _ffi
+
+FAMILY_MVN = 0
+FAMILY_SHELLS = 1
+FAMILY_LINGAUSS = 2
+PRIOR_UNIFORM = 0
+PRIOR_NORMAL = 1
+
+STATUS_BITS = {1: "init rejection budget exhausted", 2: "slice shrink budget exhausted",
+               4: "store full", 8: "bad parameter (uniform phase would need iterations)"}
+
+_TC_NAMES = ("ess", "evidence_uncert", "dlogZ", "max_samples", "max_num_likelihood_evaluations",
+             "log_L_contour", "efficiency_threshold", "rtol", "atol", "peak_XL_frac")
+_TC_FIELDS = ("ess", "evidence_uncert", "dlogZ", "max_samples", "max_nlik", "log_L_contour",
+              "efficiency_threshold", "rtol", "atol", "peak_XL_frac")
+_TC_FLAGS = ("has_ess", "has_evidence_uncert", "has_dlogZ", "has_max_samples", "has_max_nlik",
+             "has_log_L_contour", "has_efficiency", "has_rtol", "has_atol", "has_peak_XL")
+
+
+@dataclass
+class RunSpec:
+    """One nested-sampling run: model tables + sampler configuration (already rounded like
+    ShardedStaticNestedSampler.__post_init__, sharded_static.py:625-650)."""
+    D: int
+    num_live_points: int
+    shell_size: int
+    num_slices: int
+    family: int
+    params: np.ndarray
+    prior_kind: np.ndarray
+    prior_a: np.ndarray
+    prior_b: np.ndarray
+    max_samples: int
+    term_cond: Dict[str, float]
+    key: np.ndarray
+    num_phantom: int = 0
+    midpoint_shrink: bool = True
+    init_efficiency_threshold: float = 0.1
+    store_U: bool = True
+    N: int = 0
+
+
+def ncoef_table(nmax: int) -> np.ndarray:
+    """FP64 shrinkage coefficients per live-point count n (the n-only terms of
+    _update_evidence_calc_op, internals/shrinkage_statistics.py:55-73)."""
+    n = np.arange(nmax + 1, dtype=np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        lnn = np.log(n)
+        lnn1 = np.log(n + 1.0)
+        lnn2 = np.log(n + 2.0)
+        T = -np.logaddexp(0.0, -lnn)
+        t = -lnn1
+        T2 = -np.logaddexp(0.0, np.log(2.0) - lnn)
+        t2 = np.log(2.0) - lnn1 - lnn2
+        tT = -np.logaddexp(0.0, -lnn) - lnn2
+    out = np.zeros((nmax + 1, 8), np.float64)
+    out[:, 0], out[:, 1], out[:, 2], out[:, 3], out[:, 4] = T, t, T2, t2, tT
+    return out
+
+
+def term_cond_struct(tc: Dict[str, float]) -> _ffi.TermCond:
+    s = _ffi.TermCond()
+    for name, field_, flag in zip(_TC_NAMES, _TC_FIELDS, _TC_FLAGS):
+        v = tc.get(name)
+        if v is None:
+            continue
+        setattr(s, flag, 1)
+        setattr(s, field_, float(v))
+    return s
+
+
+def _dbucket(D: int) -> int:
+    if D <= 8:
+        return 0
+    if D <= 16:
+        return 1
+    if D <= 32:
+        return 2
+    if D <= 64:
+        return 3
+    raise ValueError(f"D={D} > 64 is not supported by the fused slice kernel")
+
+
+def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
+    return None if t is None else t.data_ptr()
+
+
+_STATE_DTYPE = np.dtype(_ffi.RunState)
+
+
+class NSBatch:
+    """Device state of R independent runs."""
+
+    def __init__(self, specs: List[RunSpec], device="cuda", chains_per_item: int = 64,
+                 max_evals_per_slice: int = 100000):
+        if not specs:
+            raise ValueError("no runs")
+        self.specs = specs
+        self.device = torch.device(device)
+        R = len(specs)
+        self.R = R
+        dev = self.device
+        Ds = np.array([s.D for s in specs])
+        ns = np.array([s.num_live_points for s in specs])
+        ss = np.array([s.shell_size for s in specs])
+        Ks = np.array([s.num_phantom for s in specs])
+        caps = np.array([s.max_samples for s in specs], np.int64)
+        if ns.max() > 4096:
+            raise ValueError("at most 4096 live points per run")
+        for s in specs:
+            if s.family not in (FAMILY_MVN, FAMILY_SHELLS):
+                raise ValueError("the slice engine runs the MVN and shells families; the linear-Gaussian "
+                                 "family uses the tensor-core path")
+            _dbucket(s.D)
+        live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])
+        store_off = np.concatenate([[0], np.cumsum(caps)[:-1]])
+        shell_off = np.concatenate([[0], np.cumsum(ss)[:-1]])
+        plen = np.array([len(s.params) for s in specs])
+        param_off = np.concatenate([[0], np.cumsum(plen)[:-1]])
+        prior_off = np.concatenate([[0], np.cumsum(Ds)[:-1]])
+        ustore = np.array([s.store_U for s in specs])
+        ucap = np.where(ustore, caps * Ds, 0)
+        ustore_off = np.where(ustore, np.concatenate([[0], np.cumsum(ucap)[:-1]]), -1)
+        excl = lambda v: np.concatenate([[0], np.cumsum(v)[:-1]]).astype(np.int64)
+        liveU_off, newU_off = excl(ns * Ds), excl(ss * Ds)
+        phU_off, phL_off = excl(ss * Ks * Ds), excl(ss * Ks)
+        self.offsets = dict(live=live_off, store=store_off, shell=shell_off, ustore=ustore_off, liveU=liveU_off,
+                            newU=newU_off)
+
+        descs = (_ffi.RunDesc * R)()
+        for r, s in enumerate(specs):
+            d = descs[r]
+            d.D, d.n, d.s, d.S, d.K = s.D, s.num_live_points, s.shell_size, s.num_slices, s.num_phantom
+            d.family, d.midpoint = s.family, int(bool(s.midpoint_shrink))
+            d.uniform_phase = int(s.init_efficiency_threshold > 0.0)
+            d.N = s.N
+            d.init_efficiency_threshold = float(s.init_efficiency_threshold)
+            d.cap = int(caps[r])
+            d.live_off, d.store_off, d.shell_off = int(live_off[r]), int(store_off[r]), int(shell_off[r])
+            d.param_off, d.prior_off, d.ustore_off = int(param_off[r]), int(prior_off[r]), int(ustore_off[r])
+            d.liveU_off, d.newU_off = int(liveU_off[r]), int(newU_off[r])
+            d.phU_off, d.phL_off = int(phU_off[r]), int(phL_off[r])
+            d.tc = term_cond_struct(s.term_cond)
+        self._descs_host = descs
+        u8 = lambda obj: torch.frombuffer(bytearray(bytes(obj)), dtype=torch.uint8)
+        self.t_runs = u8(descs).to(dev)
+        self.t_state = torch.zeros(R * ctypes.sizeof(_ffi.RunState), dtype=torch.uint8, device=dev)
+        st = (_ffi.RunState * R)()
+        for r, s in enumerate(specs):
+            st[r].key[0], st[r].key[1] = int(s.key[0]), int(s.key[1])
+        self.t_state.copy_(u8(st))
+        self.t_state0 = self.t_state.clone()
+        self._state_host0 = u8(st).pin_memory() if torch.cuda.is_available() else u8(st)
+
+        nsum, ssum, capsum = int(ns.sum()), int(ss.sum()), int(caps.sum())
+        nD = int((ns * Ds).sum())
+        f32, i32 = torch.float32, torch.int32
+        z = lambda *shape, dtype=f32: torch.zeros(*shape, dtype=dtype, device=dev)
+        self.live_U = [z(nD), z(nD)]
+        self.live_L = [z(nsum), z(nsum)]
+        self.live_Lc = [z(nsum), z(nsum)]
+        self.live_E = [z(nsum, dtype=i32), z(nsum, dtype=i32)]
+        self.live_S = [z(nsum, dtype=i32), z(nsum, dtype=i32)]
+        self.new_U = z(int((ss * Ds).sum()))
+        self.new_L = z(ssum)
+        self.new_E = z(ssum, dtype=i32)
+        self.ph_U = z(max(int((ss * Ks * Ds).sum()), 1))
+        self.ph_L = z(max(int((ss * Ks).sum()), 1))
+        self.store_L = torch.full((capsum,), float("inf"), dtype=f32, device=dev)
+        self.store_S = z(capsum, dtype=i32)
+        self.store_E = z(capsum, dtype=i32)
+        self.store_P = z(capsum, dtype=torch.uint8)
+        usum = int(ucap.sum())
+        self.store_U = z(usum) if usum > 0 else None
+        self.fparams = torch.from_numpy(np.concatenate([np.asarray(s.params, np.float32) for s in specs])).to(dev)
+        self.prior_kind = torch.from_numpy(np.concatenate([np.asarray(s.prior_kind, np.int32) for s in specs])).to(dev)
+        self.prior_a = torch.from_numpy(np.concatenate([np.asarray(s.prior_a, np.float32) for s in specs])).to(dev)
+        self.prior_b = torch.from_numpy(np.concatenate([np.asarray(s.prior_b, np.float32) for s in specs])).to(dev)
+        self.nmax = int(ns.max())
+        # tree counts can exceed n (the sender convention of _collect_shell); cover n + 64 and
+        # let the device compute larger counts' coefficients on the fly
+        self.ncoef_n = self.nmax + 64
+        self.ncoef = torch.from_numpy(ncoef_table(self.ncoef_n)).to(dev)
+
+        # work items: (run, first chain, chain count), grouped by (family, D bucket),
+        # longest (largest D) first inside a bucket
+        CH = int(chains_per_item)
+        items = []
+        for r, s in enumerate(specs):
+            b = s.family * 4 + _dbucket(s.D)
+            for c0 in range(0, s.shell_size, CH):
+                items.append((b, -s.D, r, c0, min(CH, s.shell_size - c0)))
+        items.sort()
+        arr = np.array([[it[2], it[3], it[4], 0] for it in items], np.int32).reshape(-1, 4)
+        self.items = torch.from_numpy(arr).to(dev)
+        bb = np.full(8, 0, np.int32)
+        be = np.full(8, 0, np.int32)
+        bk = np.array([it[0] for it in items])
+        for k in range(8):
+            idx = np.nonzero(bk == k)[0]
+            if len(idx):
+                bb[k], be[k] = idx[0], idx[-1] + 1
+        b = _ffi.Batch()
+        b.num_runs, b.nmax, b.ncoef_n = R, self.nmax, self.ncoef_n
+        b.runs, b.state = _ptr(self.t_runs), _ptr(self.t_state)
+        for p in range(2):
+            b.live_U[p], b.live_L[p], b.live_Lc[p] = _ptr(self.live_U[p]), _ptr(self.live_L[p]), _ptr(self.live_Lc[p])
+            b.live_E[p], b.live_S[p] = _ptr(self.live_E[p]), _ptr(self.live_S[p])
+        b.new_U, b.new_L, b.new_E = _ptr(self.new_U), _ptr(self.new_L), _ptr(self.new_E)
+        b.ph_U, b.ph_L = _ptr(self.ph_U), _ptr(self.ph_L)
+        b.store_L, b.store_S, b.store_E, b.store_P = (_ptr(self.store_L), _ptr(self.store_S), _ptr(self.store_E),
+                                                      _ptr(self.store_P))
+        b.store_U = _ptr(self.store_U)
+        b.fparams, b.prior_kind, b.prior_a, b.prior_b = (_ptr(self.fparams), _ptr(self.prior_kind),
+                                                         _ptr(self.prior_a), _ptr(self.prior_b))
+        b.ncoef, b.items, b.num_items = _ptr(self.ncoef), _ptr(self.items), len(items)
+        for k in range(8):
+            b.bucket_begin[k], b.bucket_end[k] = int(bb[k]), int(be[k])
+        b.chains_per_item = CH
+        b.max_evals_per_slice = int(max_evals_per_slice)
+        self._b = b
+        self._graphs: Dict[tuple, tuple] = {}
+        self.timing = False
+        self.shell_ms = 0.0
+        self.shell_launch_groups = 0
+        self.iterations_run = 0
+        self.kernel_launches = 0
+        self._kernels_per_iter = 1 + int(np.count_nonzero(be > bb))
+
+    # ----------------------------------------------------------------- driving
+    @staticmethod
+    def _stream():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def init(self):
+        _ffi.call("gbns_batch_init", ctypes.byref(self._b), self._stream())
+        self.kernel_launches += 2
+
+    def iterate(self, k: int):
+        _ffi.call("gbns_batch_iterate", ctypes.byref(self._b), int(k), self._stream())
+        self.iterations_run += k
+        self.kernel_launches += k * self._kernels_per_iter
+
+    def _graph(self, k: int):
+        """CUDA graph of k iterations; when timing, each iteration is captured as
+        [event, shell kernels, event, merge kernel] so the slice sampler's device time is
+        read back from events recorded by the graph itself."""
+        key = (k, self.timing)
+        ent = self._graphs.get(key)
+        if ent is None:
+            g = torch.cuda.CUDAGraph()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(k)] if self.timing else []
+            for a, b_ in evs:  # materialise the lazily created events before capture
+                a.record()
+                b_.record()
+            torch.cuda.current_stream().synchronize()
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.graph(g, stream=side):
+                if self.timing:
+                    for a, b_ in evs:
+                        _ffi.call("gbns_record_event", ctypes.c_void_p(a.cuda_event), self._stream())
+                        _ffi.call("gbns_batch_shell", ctypes.byref(self._b), self._stream())
+                        _ffi.call("gbns_record_event", ctypes.c_void_p(b_.cuda_event), self._stream())
+                        _ffi.call("gbns_batch_merge", ctypes.byref(self._b), self._stream())
+                else:
+                    _ffi.call("gbns_batch_iterate", ctypes.byref(self._b), int(k), self._stream())
+            torch.cuda.current_stream().wait_stream(side)
+            ent = (g, evs)
+            self._graphs[key] = ent
+        return ent
+
+    def iterate_graph(self, k: int):
+        g, evs = self._graph(k)
+        g.replay()
+        self.iterations_run += k
+        self.kernel_launches += k * self._kernels_per_iter
+        self._pending_events = evs
+
+    def _collect_timing(self):
+        evs = getattr(self, "_pending_events", None)
+        if evs:
+            self.shell_ms += sum(a.elapsed_time(b_) for a, b_ in evs)
+            self.shell_launch_groups += len(evs)
+        self._pending_events = None
+
+    def reset(self, from_host: bool = False):
+        """Restore every run's initial state (keys); from_host copies it from pinned memory."""
+        if from_host:
+            self.t_state.copy_(self._state_host0, non_blocking=True)
+        else:
+            self.t_state.copy_(self.t_state0)
+        self.store_L.fill_(float("inf"))
+
+    def state(self) -> np.ndarray:
+        return np.frombuffer(self.t_state.cpu().numpy().tobytes(), dtype=_STATE_DTYPE)
+
+    def all_done(self) -> bool:
+        st = self.state()
+        return bool(np.all(st["done"] != 0))
+
+    def finalize(self):
+        _ffi.call("gbns_batch_finalize", ctypes.byref(self._b), self._stream())
+        self.kernel_launches += 1
+
+    def run(self, block: int = 8, max_iterations: Optional[int] = None, use_graph: bool = True,
+            check: bool = True) -> np.ndarray:
+        """Run every run to termination; returns the final per-run state records."""
+        self.init()
+        if max_iterations is None:
+            max_iterations = int(max(s.max_samples // max(s.shell_size, 1) + 2 for s in self.specs))
+        done_it = 0
+        while done_it < max_iterations:
+            done = self.all_done()
+            self._collect_timing()
+            if done:
+                break
+            k = min(block, max_iterations - done_it)
+            if use_graph:
+                self.iterate_graph(k)
+            else:
+                self.iterate(k)
+            done_it += k
+        self.finalize()
+        st = self.state()
+        self._collect_timing()
+        if not check:
+            return st
+        bad = st["status"] != 0
+        if np.any(bad):
+            r = int(np.nonzero(bad)[0][0])
+            msgs = [m for bit, m in STATUS_BITS.items() if st["status"][r] & bit]
+            raise _ffi.GBNSError(f"run {r}: device status {st['status'][r]} ({'; '.join(msgs)})")
+        if not np.all(st["phase"] == 2):
+            raise _ffi.GBNSError("iteration budget exhausted before termination")
+        return st
+
+    # ----------------------------------------------------------------- results
+    def results(self, with_U: bool = True) -> Dict[str, torch.Tensor]:
+        dev = self.device
+        caps = np.array([s.max_samples for s in self.specs], np.int64)
+        capsum = int(caps.sum())
+        R = self.R
+        z = lambda n, dt: torch.zeros(n, dtype=dt, device=dev)
+        out = dict(samples_indices=z(capsum, torch.int32), num_live_points=z(capsum, torch.int32),
+                   log_L_samples=z(capsum, torch.float32), log_dp_mean=z(capsum, torch.float64),
+                   log_X_mean=z(capsum, torch.float64), nevals_sorted=z(capsum, torch.int32),
+                   scalars=z(R * 8, torch.float64))
+        out["U_sorted"] = z(self.store_U.numel(), torch.float32) if (with_U and self.store_U is not None) else None
+        scratch_ll = z(2 * (capsum + R), torch.int64)
+        scratch_i = z(capsum + R, torch.int32)
+        rb = _ffi.ResultsBufs()
+        rb.samples_indices, rb.num_live_points = _ptr(out["samples_indices"]), _ptr(out["num_live_points"])
+        rb.log_L_samples, rb.log_dp_mean = _ptr(out["log_L_samples"]), _ptr(out["log_dp_mean"])
+        rb.log_X_mean, rb.nevals_sorted = _ptr(out["log_X_mean"]), _ptr(out["nevals_sorted"])
+        rb.U_sorted, rb.scalars = _ptr(out["U_sorted"]), _ptr(out["scalars"])
+        rb.scratch_ll, rb.scratch_i = _ptr(scratch_ll), _ptr(scratch_i)
+        _ffi.call("gbns_batch_results", ctypes.byref(self._b), ctypes.byref(rb), self._stream())
+        self.kernel_launches += 1
+        out["scalars"] = out["scalars"].view(R, 8)
+        return out
+
+    def run_slices(self, r: int, out: Dict[str, torch.Tensor]) -> Dict[str, torch.Tensor]:
+        """Per-run views (trimmed to the run's sample count) of a results() dict."""
+        st = self.state()
+        s = self.specs[r]
+        o = int(self.offsets["store"][r])
+        N = int(min(st["num_samples"][r], s.max_samples))
+        d = {k: v[o:o + N] for k, v in out.items() if k not in ("scalars", "U_sorted") and v is not None}
+        if out.get("U_sorted") is not None and self.offsets["ustore"][r] >= 0:
+            uo = int(self.offsets["ustore"][r])
+            d["U_sorted"] = out["U_sorted"][uo:uo + N * s.D].view(N, s.D)
+        d["scalars"] = out["scalars"][r]
+        return d
+
+    def store_view(self, r: int) -> Dict[str, torch.Tensor]:
+        st = self.state()
+        s = self.specs[r]
+        o = int(self.offsets["store"][r])
+        N = int(min(st["num_samples"][r], s.max_samples))
+        d = dict(log_L=self.store_L[o:o + N], sender=self.store_S[o:o + N], nevals=self.store_E[o:o + N],
+                 phantom=self.store_P[o:o + N])
+        if self.store_U is not None and self.offsets["ustore"][r] >= 0:
+            uo = int(self.offsets["ustore"][r])
+            d["U"] = self.store_U[uo:uo + N * s.D].view(N, s.D)
+        return d
+
+    def live_view(self, r: int) -> Dict[str, torch.Tensor]:
+        st = self.state()
+        p = int(st["parity"][r])
+        s = self.specs[r]
+        o = int(self.offsets["live"][r])
+        uo = int(self.offsets["liveU"][r])
+        n = s.num_live_points
+        return dict(U=self.live_U[p][uo:uo + n * s.D].view(n, s.D), log_L=self.live_L[p][o:o + n],
+                    nevals=self.live_E[p][o:o + n], sender=self.live_S[p][o:o + n],
+                    log_L_constraint=self.live_Lc[p][o:o + n])
+
+    def forward(self, r: int, U: torch.Tensor) -> torch.Tensor:
+        """Model.forward of run r over a batch U [B, D] (device tensor)."""
+        U = U.to(device=self.device, dtype=torch.float32).contiguous()
+        out = torch.empty(U.shape[0], dtype=torch.float32, device=self.device)
+        _ffi.call("gbns_forward", ctypes.byref(self._b), int(r), ctypes.c_void_p(U.data_ptr()),
+                  ctypes.c_void_p(out.data_ptr()), ctypes.c_longlong(U.shape[0]), self._stream())
+        return out
+
+    def slice_shell(self, Lstar: torch.Tensor, keys: torch.Tensor):
+        """One shell of every run from the current live sets with explicit contours and
+        sample keys (test hook): outputs in new_U / new_L / new_E."""
+        Lstar = Lstar.to(device=self.device, dtype=torch.float32).contiguous()
+        keys = keys.to(device=self.device, dtype=torch.int32).contiguous()
+        _ffi.call("gbns_slice_shell", ctypes.byref(self._b), ctypes.c_void_p(Lstar.data_ptr()),
+                  ctypes.c_void_p(keys.data_ptr()), self._stream())
+
+    def set_live(self, r: int, U: np.ndarray, log_L: np.ndarray):
+        """Overwrite run r's current live set (test hook; values must be sorted by log_L)."""
+        st = self.state()
+        p = int(st["parity"][r])
+        s = self.specs[r]
+        o = int(self.offsets["live"][r])
+        uo = int(self.offsets["liveU"][r])
+        n = s.num_live_points
+        self.live_U[p][uo:uo + n * s.D].copy_(torch.from_numpy(np.asarray(U, np.float32).ravel()))
+        self.live_L[p][o:o + n].copy_(torch.from_numpy(np.asarray(log_L, np.float32)))
+
+
+# --------------------------------------------------------------- model tables
+
+def mvn_params(mu, cov) -> np.ndarray:
+    """[mu, Linv (row-major lower), c0] with L = chol(cov), c0 = -sum log L_ii - D/2 log 2 pi."""
+    mu = np.asarray(mu, np.float64)
+    L = np.linalg.cholesky(np.asarray(cov, np.float64))
+    Linv = np.linalg.inv(L)
+    Linv = np.tril(Linv)
+    D = len(mu)
+    c0 = -np.sum(np.log(np.diag(L))) - 0.5 * D * np.log(2.0 * np.pi)
+    return np.concatenate([mu, Linv.ravel(), [c0]]).astype(np.float32)
+
+
+def shells_params(c1, c2, radius, width) -> np.ndarray:
+    norm = np.log(np.sqrt(2.0 * np.pi * width ** 2))
+    return np.concatenate([np.asarray(c1, np.float64), np.asarray(c2, np.float64),
+                           [radius, width, norm]]).astype(np.float32)

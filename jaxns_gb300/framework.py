@@ -1,0 +1,161 @@
+"""Modelling front end: ``Prior`` / ``Model`` with jaxns's generator-based prior syntax
+(framework/model.py:24-41, framework/prior.py:65, framework/ops.py:89-326).
+
+A fused CUDA likelihood cannot be an arbitrary Python callable, so ``log_likelihood`` is
+one of the registered likelihood families of :mod:`jaxns_gb300.likelihoods`; priors are
+Uniform or Normal quantile transforms per U dimension (the quantiles jaxns applies through
+WrappedTFPDistribution._forward, framework/wrapped_tfp_distribution.py:77-84).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Callable, List, Optional, Sequence
+
+import numpy as np
+
+from .engine import PRIOR_NORMAL, PRIOR_UNIFORM
+
+
+class InvalidPriorName(Exception):
+    def __init__(self, name: Optional[str] = None):
+        super().__init__(f'Prior name {name} already taken by another prior.')
+
+
+class Uniform:
+    """Uniform(low, high) distribution (quantile: low + (high - low) * u)."""
+
+    def __init__(self, low, high):
+        self.low = np.asarray(low, np.float64)
+        self.high = np.asarray(high, np.float64)
+        self.shape = np.broadcast(self.low, self.high).shape
+
+    def table(self):
+        size = int(np.prod(self.shape)) if self.shape else 1
+        a = np.broadcast_to(self.low, self.shape).ravel() if self.shape else np.array([float(self.low)])
+        b = (np.broadcast_to(self.high, self.shape).ravel() - a) if self.shape else \
+            np.array([float(self.high) - float(self.low)])
+        return np.full(size, PRIOR_UNIFORM, np.int32), a, b
+
+
+class Normal:
+    """Normal(loc, scale) distribution (quantile: loc + scale * ndtri(u))."""
+
+    def __init__(self, loc, scale):
+        self.loc = np.asarray(loc, np.float64)
+        self.scale = np.asarray(scale, np.float64)
+        self.shape = np.broadcast(self.loc, self.scale).shape
+
+    def table(self):
+        size = int(np.prod(self.shape)) if self.shape else 1
+        a = np.broadcast_to(self.loc, self.shape).ravel() if self.shape else np.array([float(self.loc)])
+        b = np.broadcast_to(self.scale, self.shape).ravel() if self.shape else np.array([float(self.scale)])
+        return np.full(size, PRIOR_NORMAL, np.int32), a, b
+
+
+class Prior:
+    """A named prior over a block of U dimensions (framework/prior.py:65)."""
+
+    def __init__(self, dist_or_value, name: Optional[str] = None):
+        if not isinstance(dist_or_value, (Uniform, Normal)):
+            raise ValueError("Prior supports Uniform and Normal distributions on the fused GPU path")
+        self.dist = dist_or_value
+        self.name = name
+
+    @property
+    def base_shape(self):
+        return self.dist.shape
+
+    @property
+    def size(self) -> int:
+        return int(np.prod(self.dist.shape)) if self.dist.shape else 1
+
+
+@dataclass
+class _ParsedPrior:
+    name: str
+    shape: tuple
+    start: int
+    size: int
+
+
+class Model:
+    """Model(prior_model, log_likelihood) (framework/model.py:24)."""
+
+    def __init__(self, prior_model: Callable, log_likelihood, params=None):
+        self.prior_model = prior_model
+        self.log_likelihood = log_likelihood
+        self._params = params
+        priors: List[_ParsedPrior] = []
+        kinds, a_s, b_s = [], [], []
+        gen = prior_model()
+        names = set()
+        start = 0
+        try:
+            p = next(gen)
+            while True:
+                if not isinstance(p, Prior):
+                    raise ValueError("prior_model must yield Prior objects")
+                name = p.name or f"__prior_{len(priors)}"
+                if name in names:
+                    raise InvalidPriorName(name)
+                names.add(name)
+                k, a, b = p.dist.table()
+                priors.append(_ParsedPrior(name, p.dist.shape, start, p.size))
+                kinds.append(k)
+                a_s.append(a)
+                b_s.append(b)
+                start += p.size
+                p = gen.send(np.zeros(p.dist.shape))
+        except StopIteration:
+            pass
+        self.priors = priors
+        self.U_ndims = start
+        self.prior_kind = np.concatenate(kinds) if kinds else np.zeros(0, np.int32)
+        self.prior_a = np.concatenate(a_s) if a_s else np.zeros(0)
+        self.prior_b = np.concatenate(b_s) if b_s else np.zeros(0)
+        if self.U_ndims < 1:
+            raise ValueError("model has no sampled dimensions")
+        log_likelihood.check(self.U_ndims)
+
+    def __call__(self, params):
+        return Model(self.prior_model, self.log_likelihood, params=params)
+
+    def transform(self, U):
+        """U -> X (dict of prior name -> value), vectorised over leading axes."""
+        X = self.transform_flat(U)
+        return {p.name: X[..., p.start:p.start + p.size].reshape(X.shape[:-1] + tuple(p.shape))
+                for p in self.priors if not p.name.startswith("__prior_")}
+
+    def transform_flat(self, U):
+        import torch
+        is_t = isinstance(U, torch.Tensor)
+        Ut = U if is_t else torch.as_tensor(np.asarray(U, np.float64))
+        a = torch.as_tensor(self.prior_a, dtype=Ut.dtype, device=Ut.device)
+        b = torch.as_tensor(self.prior_b, dtype=Ut.dtype, device=Ut.device)
+        normal = torch.as_tensor(self.prior_kind == PRIOR_NORMAL, device=Ut.device)
+        q = torch.where(normal, np.sqrt(2.0) * torch.erfinv(2.0 * Ut - 1.0), Ut)
+        X = a + b * q
+        return X if is_t else X.numpy()
+
+    def log_prob_prior(self, U):
+        """log prior density of the X that U maps to (per sample)."""
+        import torch
+        X = self.transform_flat(U)
+        a = torch.as_tensor(self.prior_a, dtype=X.dtype, device=X.device)
+        b = torch.as_tensor(self.prior_b, dtype=X.dtype, device=X.device)
+        normal = torch.as_tensor(self.prior_kind == PRIOR_NORMAL, device=X.device)
+        inside = (X >= a) & (X <= a + b)
+        lp_u = torch.where(inside, -torch.log(b), torch.full_like(X, -float("inf")))
+        lp_n = -0.5 * ((X - a) / b) ** 2 - torch.log(b) - 0.5 * np.log(2.0 * np.pi)
+        return torch.where(normal, lp_n, lp_u).sum(-1)
+
+    @property
+    def U_placeholder(self):
+        return np.zeros(self.U_ndims)
+
+    def family_params(self) -> np.ndarray:
+        return self.log_likelihood.params(self)
+
+    @property
+    def family(self) -> int:
+        return self.log_likelihood.family

@@ -1,0 +1,193 @@
+"""GPU parity: libgbns.so (through its C ABI) against the FP64 oracle on seeded inputs."""
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests.conftest import corr_gauss
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _s():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _spec(D, n, S, seed_key, family=0, params=None, cap=None, tc=None, K=0, store_U=True, seed=0, low=-10., high=10.):
+    from jaxns_gb300.engine import RunSpec, mvn_params
+    mu, cov = corr_gauss(D, seed)
+    if params is None:
+        params = mvn_params(mu, cov)
+    s = n // 2
+    cap = cap or 100 * n
+    cap = int(np.ceil(cap / (s * (1 + K))) * s * (1 + K))
+    return RunSpec(D=D, num_live_points=n, shell_size=s, num_slices=S, family=family, params=params,
+                   prior_kind=np.zeros(D, np.int32), prior_a=np.full(D, low), prior_b=np.full(D, high - low),
+                   max_samples=cap, term_cond=dict(tc or {"dlogZ": 1e-4, "max_samples": float(cap)}),
+                   key=np.asarray(seed_key, np.uint32), num_phantom=K, store_U=store_U), (mu, cov)
+
+
+def test_rng_words_exact(gpu_lib, oracle_mod):
+    from jaxns_gb300 import _ffi
+    key = torch.tensor(np.array([0x13198a2e, 0x03707344], np.uint32).view(np.int32), device="cuda")
+    ctr = torch.tensor(np.array([0x243f6a88, 0x85a308d3, 0, 0, 0xffffffff, 0xffffffff], np.uint32).view(np.int32),
+                       device="cuda")
+    out = torch.zeros(6, dtype=torch.int32, device="cuda")
+    _ffi.call("gbns_threefry2x32", _p(key), _p(ctr), _p(out), ctypes.c_longlong(3), _s())
+    got = out.cpu().numpy().view(np.uint32)
+    assert (got[0], got[1]) == (0xc4923a9c, 0x483df7a0)
+    for seed in (0, 1, 12345):
+        k = oracle_mod.PRNGKey(seed)
+        kt = torch.tensor(k.view(np.int32), device="cuda")
+        n = 4099
+        sp = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
+        _ffi.call("gbns_threefry_split", _p(kt), _p(sp), ctypes.c_longlong(n), _s())
+        np.testing.assert_array_equal(sp.cpu().numpy().view(np.uint32).reshape(n, 2), oracle_mod.split(k, n))
+        bits = torch.zeros(n, dtype=torch.int64, device="cuda")
+        _ffi.call("gbns_random_bits64", _p(kt), _p(bits), ctypes.c_longlong(n), _s())
+        np.testing.assert_array_equal(bits.cpu().numpy().view(np.uint64), oracle_mod.random_bits64(k, n))
+
+
+def test_uniform_normal_values(gpu_lib, oracle_mod):
+    from jaxns_gb300 import _ffi
+    n = 20000
+    k = oracle_mod.PRNGKey(99)
+    kt = torch.tensor(k.view(np.int32), device="cuda")
+    u = torch.zeros(n, device="cuda")
+    z = torch.zeros(n, device="cuda")
+    _ffi.call("gbns_uniform", _p(kt), _p(u), ctypes.c_longlong(n), _s())
+    _ffi.call("gbns_normal", _p(kt), _p(z), ctypes.c_longlong(n), _s())
+    uo = oracle_mod.uniform(k, n)
+    zo = oracle_mod.normal(k, n)
+    # fp32 rounding of the f64 variates (tolerance: 1 ulp of fp32 for uniform, 4e-7 rel for normal)
+    np.testing.assert_allclose(u.cpu().numpy(), uo, rtol=6e-8, atol=0)
+    np.testing.assert_allclose(z.cpu().numpy(), zo, rtol=4e-6, atol=1e-7)
+
+
+def test_forward_matches_oracle(gpu_lib, oracle_mod):
+    from jaxns_gb300.engine import NSBatch, shells_params
+    for D in (2, 8, 13, 37, 64):
+        spec, (mu, cov) = _spec(D, 64, D, oracle_mod.PRNGKey(0), seed=D)
+        b = NSBatch([spec])
+        U = np.random.default_rng(D).uniform(0.3, 0.7, size=(257, D))
+        got = b.forward(0, torch.tensor(U, dtype=torch.float32)).cpu().numpy()
+        om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+        ref = oracle_mod.forward(om, U.astype(np.float32).astype(np.float64))
+        np.testing.assert_allclose(got, ref, rtol=2e-4, atol=2e-3)
+    D = 10
+    c1 = np.zeros(D); c1[0] = 3.5
+    c2 = -c1
+    spec, _ = _spec(D, 64, D, oracle_mod.PRNGKey(0), family=1, params=shells_params(c1, c2, 2.0, 0.1), low=-6., high=6.)
+    b = NSBatch([spec])
+    U = np.random.default_rng(0).uniform(0, 1, size=(300, D))
+    U[:100] = (np.concatenate([[3.5 + 2.0], np.zeros(D - 1)]) + 6) / 12 + 0.01 * np.random.default_rng(1).standard_normal((100, D))
+    got = b.forward(0, torch.tensor(U, dtype=torch.float32)).cpu().numpy()
+    om = oracle_mod.shells_model(-6, 6, c1, c2, 2.0, 0.1)
+    ref = oracle_mod.forward(om, U.astype(np.float32).astype(np.float64))
+    np.testing.assert_allclose(got, ref, rtol=2e-4, atol=5e-3)
+
+
+def test_init_live_points_match_oracle(gpu_lib, oracle_mod):
+    from jaxns_gb300.engine import NSBatch
+    for D, n in ((2, 64), (8, 512), (33, 200)):
+        key = oracle_mod.PRNGKey(D * 7 + 1)
+        spec, (mu, cov) = _spec(D, n, D, key, seed=D)
+        b = NSBatch([spec])
+        b.init()
+        live = b.live_view(0)
+        om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+        orun = oracle_mod.ns_run(om, key, n, D, init_only=True)
+        np.testing.assert_allclose(live["U"].cpu().numpy(), orun.register["live_U"], rtol=0, atol=6e-8)
+        np.testing.assert_allclose(live["log_L"].cpu().numpy(), orun.register["live_log_L"], rtol=2e-4, atol=2e-3)
+        st = b.state()[0]
+        np.testing.assert_array_equal(np.array(st["key"], np.uint32), orun.register["key"])
+
+
+@pytest.mark.parametrize("D,n,S", [(2, 64, 8), (8, 512, 32), (10, 200, 50), (24, 128, 24), (64, 96, 64)])
+def test_slice_shell_chain_parity(gpu_lib, oracle_mod, D, n, S):
+    """One shell from the same live set, contour and key: every chain's RNG stream is the
+    reference's, so nevals and the accepted point agree chain by chain; a chain may only
+    diverge where an fp32 likelihood comparison flips against the FP64 oracle."""
+    from jaxns_gb300.engine import NSBatch
+    key = oracle_mod.PRNGKey(D)
+    spec, (mu, cov) = _spec(D, n, S, key, seed=D)
+    b = NSBatch([spec])
+    b.init()
+    live = b.live_view(0)
+    s = n // 2
+    Lstar = float(live["log_L"][s - 1].item())
+    skey = oracle_mod.PRNGKey(1000 + D)
+    b.slice_shell(torch.tensor([Lstar]), torch.tensor(skey.view(np.int32)).view(1, 2))
+    torch.cuda.synchronize()
+    om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    U_o, L_o, E_o = oracle_mod.slice_shell(om, skey, Lstar, live["U"].cpu().double().numpy(),
+                                           live["log_L"].cpu().double().numpy(), s, S)
+    E_g = b.new_E[:s].cpu().numpy()
+    U_g = b.new_U[:s * D].view(s, D).cpu().numpy()
+    L_g = b.new_L[:s].cpu().numpy()
+    same = (E_g == E_o) & np.all(np.abs(U_g - U_o) < 2e-4, axis=1)
+    assert same.mean() >= 0.95, f"chain parity {same.mean():.3f}"
+    np.testing.assert_allclose(L_g[same], L_o[same], rtol=1e-3, atol=1e-2)
+    assert np.all(L_g > Lstar)
+
+
+def test_count_crossed_edges_exact(gpu_lib, oracle_mod):
+    from jaxns_gb300 import _ffi
+    rng = np.random.default_rng(5)
+    cases = [([0, 0, 0, 1, 2, 3], [1, 2, 3, 4, 5, 6]), ([0, 0, 0, 1, 3, 2], [1, 2, 3, 4, 6, 5])]
+    # a random tree (unsorted store, ties, -0/+0) and a big sorted one
+    N = 5000
+    sender = rng.integers(0, N // 2, size=N)
+    L = np.round(rng.standard_normal(N), 2).astype(np.float32)
+    L[:10] = 0.0
+    L[10:20] = -0.0
+    cases.append((sender, L))
+    N2 = 200000
+    L2 = np.sort(rng.standard_normal(N2)).astype(np.float32)
+    cases.append((np.minimum(np.arange(N2), rng.integers(0, N2, size=N2)), L2))
+    for sender, L in cases:
+        sender = np.asarray(sender, np.int32)
+        L = np.asarray(L, np.float32)
+        N = len(L)
+        ts, tL = torch.tensor(sender, device="cuda"), torch.tensor(L, device="cuda")
+        si = torch.zeros(N, dtype=torch.int32, device="cuda")
+        nl = torch.zeros(N, dtype=torch.int32, device="cuda")
+        sll = torch.zeros(2 * (N + 1), dtype=torch.int64, device="cuda")
+        si_ = torch.zeros(N + 1, dtype=torch.int32, device="cuda")
+        _ffi.call("gbns_count_crossed_edges", _p(ts), _p(tL), ctypes.c_longlong(N), _p(si), _p(nl), _p(sll), _p(si_),
+                  _s())
+        osi, onl = oracle_mod.count_crossed_edges(sender, L.astype(np.float64))
+        np.testing.assert_array_equal(si.cpu().numpy(), osi)
+        np.testing.assert_array_equal(nl.cpu().numpy(), onl)
+
+
+def test_evidence_stats_fp64(gpu_lib, oracle_mod):
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.engine import ncoef_table
+    rng = np.random.default_rng(3)
+    for N, n in ((37, 10), (20000, 500), (70001, 3200)):
+        L = np.sort(rng.standard_normal(N) * 30).astype(np.float32)
+        nl = np.full(N, n, np.int32)
+        nl[-n:] = np.arange(n, 0, -1)
+        tab = torch.tensor(ncoef_table(4096), device="cuda")
+        tL, tn = torch.tensor(L, device="cuda"), torch.tensor(nl, device="cuda")
+        fin = torch.zeros(8, dtype=torch.float64, device="cuda")
+        lX = torch.zeros(N, dtype=torch.float64, device="cuda")
+        ldZ = torch.zeros(N, dtype=torch.float64, device="cuda")
+        lZ = torch.zeros(N, dtype=torch.float64, device="cuda")
+        _ffi.call("gbns_evidence_stats", _p(tL), _p(tn), ctypes.c_longlong(N), _p(tab), ctypes.c_int(4096), _p(fin),
+                  _p(lX), _p(ldZ), _p(lZ), _s())
+        ofin, oper = oracle_mod.compute_evidence_stats(L.astype(np.float64), nl.astype(np.float64))
+        f = fin.cpu().numpy()
+        names = ("log_L", "log_X_mean", "log_X2_mean", "log_Z_mean", "log_ZX_mean", "log_Z2_mean", "log_dZ_mean",
+                 "log_dZ2_mean")
+        for i, nm in enumerate(names):
+            np.testing.assert_allclose(f[i], ofin[nm], rtol=1e-6, atol=1e-6, err_msg=nm)
+        np.testing.assert_allclose(lX.cpu().numpy(), oper["log_X_mean"], rtol=1e-12, atol=1e-9)
+        np.testing.assert_allclose(ldZ.cpu().numpy(), oper["log_dZ_mean"], rtol=1e-6, atol=1e-5)
+        np.testing.assert_allclose(lZ.cpu().numpy(), oper["log_Z_mean"], rtol=1e-6, atol=1e-5)

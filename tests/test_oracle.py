@@ -1,0 +1,178 @@
+"""CPU tests of the FP64 oracle against the reference's own known answers and against
+independent implementations (Random123 KAT vectors, scipy, analytic evidences)."""
+import numpy as np
+import pytest
+
+from tests.conftest import corr_gauss
+
+
+# Random123 known-answer vectors for threefry2x32_20 (also used by JAX's own threefry test)
+KAT = [((0x00000000, 0x00000000), (0x00000000, 0x00000000), (0x6b200159, 0x99ba4efe)),
+       ((0xffffffff, 0xffffffff), (0xffffffff, 0xffffffff), (0x1cb996fc, 0xbb002be7)),
+       ((0x13198a2e, 0x03707344), (0x243f6a88, 0x85a308d3), (0xc4923a9c, 0x483df7a0))]
+
+
+@pytest.mark.parametrize("key,ctr,expected", KAT)
+def test_threefry_kat(oracle_mod, key, ctr, expected):
+    assert tuple(int(x) for x in oracle_mod.threefry2x32(key, ctr)) == expected
+
+
+@pytest.mark.parametrize("key,ctr,expected", KAT)
+def test_host_threefry_kat(key, ctr, expected):
+    from jaxns_gb300 import random as grandom
+    a, b = grandom.threefry2x32(key, np.uint32([ctr[0]]), np.uint32([ctr[1]]))
+    assert (int(a[0]), int(b[0])) == expected
+
+
+def test_host_split_matches_oracle(oracle_mod):
+    from jaxns_gb300 import random as grandom
+    for seed in (0, 1, 42, 2**33 + 5):
+        k = grandom.PRNGKey(seed)
+        np.testing.assert_array_equal(grandom.split(k, 7), oracle_mod.split(k, 7))
+
+
+def test_prngkey_layout():
+    from jaxns_gb300 import random as grandom
+    np.testing.assert_array_equal(grandom.PRNGKey(42), [0, 42])
+    np.testing.assert_array_equal(grandom.PRNGKey(2**32 + 3), [1, 3])
+
+
+def test_erfinv_against_scipy(oracle_mod):
+    sp = pytest.importorskip("scipy.special")
+    u = np.concatenate([np.linspace(-0.999999, 0.999999, 2001), [1e-300, -1e-17, 1 - 2**-53, -1 + 2**-53]])
+    ref = sp.erfinv(u)
+    got = oracle_mod.erfinv(u)
+    np.testing.assert_allclose(got, ref, rtol=4e-15, atol=0)
+
+
+def test_uniform_and_normal_moments(oracle_mod):
+    k = oracle_mod.PRNGKey(3)
+    u = oracle_mod.uniform(k, 20000)
+    assert 0 <= u.min() and u.max() < 1
+    assert abs(u.mean() - 0.5) < 0.01
+    z = oracle_mod.normal(k, 20000)
+    assert abs(z.mean()) < 0.03 and abs(z.std() - 1) < 0.03
+
+
+def test_count_crossed_edges_reference_goldens(oracle_mod):
+    # internals/tests/test_tree_structure.py:19-30 (test_naive)
+    si, nl = oracle_mod.count_crossed_edges([0, 0, 0, 1, 2, 3], [1, 2, 3, 4, 5, 6])
+    np.testing.assert_array_equal(si, [0, 1, 2, 3, 4, 5])
+    np.testing.assert_array_equal(nl, [3, 3, 3, 3, 2, 1])
+    # second tree of test_basic (:33-49): samples 4,5 swapped in log L
+    si, nl = oracle_mod.count_crossed_edges([0, 0, 0, 1, 3, 2], [1, 2, 3, 4, 6, 5])
+    np.testing.assert_array_equal(si, [0, 1, 2, 3, 5, 4])
+    np.testing.assert_array_equal(nl, [3, 3, 3, 3, 2, 1])
+
+
+def test_count_crossed_edges_num_samples(oracle_mod):
+    # test_with_num_samples (:52-70): +inf padding rows get count 0 and the rest equals the trimmed tree
+    s1 = [0, 0, 0, 1, 2, 3, 4, 5, 0, 0]
+    l1 = [1, 2, 3, 4, 5, 6, 7, 8, np.inf, np.inf]
+    si1, nl1 = oracle_mod.count_crossed_edges(s1, l1, num_samples=8)
+    si2, nl2 = oracle_mod.count_crossed_edges(s1[:8], l1[:8])
+    np.testing.assert_array_equal(si1[:8], si2)
+    np.testing.assert_array_equal(nl1[:8], nl2)
+    np.testing.assert_array_equal(nl1[8:], 0)
+
+
+def _naive_counts(sender, log_L):
+    # count_intervals_naive (tree_structure.py:136-206): live points = samples whose
+    # constraint interval contains each sample's log L
+    log_L = np.asarray(log_L, float)
+    nodes = np.concatenate([[-np.inf], log_L])
+    cons = nodes[np.asarray(sender)]
+    order = np.argsort(log_L, kind="stable")
+    counts = []
+    for i in order:
+        counts.append(int(np.sum((cons < log_L[i]) & (log_L >= log_L[i]))))
+    return order, np.array(counts)
+
+
+def test_count_crossed_edges_random_tree(oracle_mod):
+    # the seeded random tree of test_random_tree (:73-103), against the naive count
+    np.random.seed(42)
+    log_L = [0.0]
+    parent = []
+    for idx in range(10):
+        log_L.append(log_L[idx] + np.random.uniform(low=0, high=1 - log_L[idx]) ** 4)
+        parent.append(idx)
+    for idx in range(10):
+        for _ in range(5):
+            log_L.append(np.random.uniform(low=log_L[idx], high=1.))
+            parent.append(idx)
+    si, nl = oracle_mod.count_crossed_edges(parent, log_L[1:])
+    order, counts = _naive_counts(parent, log_L[1:])
+    np.testing.assert_array_equal(si, order)
+    np.testing.assert_array_equal(nl, counts)
+
+
+def test_stable_argsort_total_order(oracle_mod):
+    keys = np.array([3.0, -0.0, np.nan, 0.0, -np.inf, np.inf, 3.0, np.nan, -1.0])
+    # jnp.argsort: -0 == +0 (stable), NaN after +inf (stable)
+    np.testing.assert_array_equal(oracle_mod.stable_argsort(keys), [4, 8, 1, 3, 0, 6, 5, 2, 7])
+
+
+def test_evidence_constant_n(oracle_mod):
+    # with n fixed, log X_i = i log(n/(n+1)) exactly in expectation (shrinkage_statistics.py:62)
+    n = 50
+    L = np.linspace(-10, 0, 400)
+    fin, per = oracle_mod.compute_evidence_stats(L, np.full(400, n))
+    i = np.arange(1, 401)
+    np.testing.assert_allclose(per["log_X_mean"], i * np.log(n / (n + 1)), rtol=1e-12)
+    # Z mean = sum X_{i-1} / (n+1) * midL
+    X = np.exp(np.concatenate([[0], per["log_X_mean"][:-1]]))
+    mid = 0.5 * (np.exp(L) + np.exp(np.concatenate([[-np.inf], L[:-1]])))
+    np.testing.assert_allclose(fin["log_Z_mean"], np.log(np.sum(X / (n + 1) * mid)), rtol=1e-12)
+
+
+def test_linear_to_log_stats(oracle_mod):
+    # internals/tests/test_stats.py:7-19 restated: log-normal moments
+    mu, var = oracle_mod.linear_to_log_stats(np.log(2.0), np.log(5.0))
+    assert np.isclose(mu, 2 * np.log(2.0) - 0.5 * np.log(5.0))
+    assert np.isclose(var, np.log(5.0) - 2 * np.log(2.0))
+
+
+def test_seed_index_integer_formula(oracle_mod):
+    """The device picks the seed as the k-th satisfying live point, k = ceil(m (1 - U)), with
+    exact 64-bit integer arithmetic; check it equals the reference's cumulative-logsumexp +
+    searchsorted (internals/random.py:34-84) on many keys."""
+    import ctypes
+    lib = oracle_mod.lib()
+    f = lib.orc_seed_index_export if hasattr(lib, "orc_seed_index_export") else None
+    assert f is not None
+    f.restype = ctypes.c_long
+    rng = np.random.default_rng(0)
+    for trial in range(300):
+        n = int(rng.integers(2, 700))
+        L = np.sort(rng.standard_normal(n))
+        s = int(rng.integers(1, n))
+        Lstar = L[s - 1]
+        key = oracle_mod.split(oracle_mod.PRNGKey(trial), 2)[1]
+        idx = f(ctypes.c_uint32(int(key[0])), ctypes.c_uint32(int(key[1])), L.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                ctypes.c_long(n), ctypes.c_double(Lstar))
+        m = int(np.sum(L > Lstar))
+        b = int(oracle_mod.random_bits64(key, 1)[0])
+        M = b >> 12
+        if m == 0:
+            expect = 0
+        else:
+            k = -((-m * ((1 << 52) - M)) >> 52)
+            expect = (n - m) + k - 1
+        assert idx == expect, (trial, n, m, idx, expect)
+
+
+def test_config1_oracle_log_Z_unbiased(oracle_mod):
+    """Config 1 (D=8 correlated Gaussian, U[-10,10]^8, 512 live points, 32 slices,
+    dlogZ<1e-4): the ensemble of oracle runs is centred on the analytic -8 log 20."""
+    D = 8
+    mu, cov = corr_gauss(D, 0)
+    m = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    R = 8
+    lz, nev, reasons = oracle_mod.ns_run_batch([m] * R, [dict(num_live_points=512, num_slices=32,
+                                                                max_samples=51200)] * R,
+                                               np.array([oracle_mod.PRNGKey(i) for i in range(R)]),
+                                               [{"dlogZ": 1e-4}] * R, 8)
+    truth = -D * np.log(20.0)
+    assert np.all(reasons == 4)
+    assert abs(lz.mean() - truth) < 3 * 0.25 / np.sqrt(R)
