@@ -87,6 +87,7 @@ typedef struct {
     int N;            /* rows of Phi (linear-Gaussian family) */
     int pad0;
     double init_efficiency_threshold;
+    double log_L_offset;   /* FP64 constant part of log L; device values are log L - log_L_offset */
     long long cap;         /* store capacity (max_samples, rounded) */
     long long live_off;    /* index of the run's first live point */
     long long store_off;   /* index of the run's first store slot */
@@ -125,7 +126,11 @@ typedef struct {
     int pad1;
 } gbns_run_state;
 
-/* device buffers of a batch of runs (all *_dev, caller-allocated) */
+/* Log-likelihoods are held on the device in fp32 relative to the run's FP64 log_L_offset
+ * (e.g. the Gaussian normalisation), so the resolution near a likelihood peak is that of
+ * -0.5 z^2 rather than of the absolute value; the shift is monotone, so every comparison,
+ * tie and sort order is that of the absolute values.  FP64 code adds the offset back.
+ * device buffers of a batch of runs (all *_dev, caller-allocated) */
 typedef struct {
     int num_runs;
     int nmax;                       /* largest n over runs (<= 4096) */
@@ -164,7 +169,7 @@ typedef struct {
 typedef struct {
     int *samples_indices;           /* [sum cap] */
     int *num_live_points;           /* [sum cap] */
-    float *log_L_samples;           /* [sum cap] sorted */
+    double *log_L_samples;          /* [sum cap] sorted, absolute (offset added in FP64) */
     double *log_dp_mean;            /* [sum cap] */
     double *log_X_mean;             /* [sum cap] */
     int *nevals_sorted;             /* [sum cap] */
@@ -211,7 +216,8 @@ int gbns_record_event(void *event, void *stream);
 int gbns_batch_merge(const gbns_batch *batch, void *stream);
 int gbns_batch_results(const gbns_batch *batch, const gbns_results_bufs *res, void *stream);
 
-/* One shell of the slice sampler for every run (test hook: no merge, no register) */
+/* One shell of the slice sampler for every run (test hook: no merge, no register);
+ * Lstar_dev holds each run's contour relative to its log_L_offset */
 int gbns_slice_shell(const gbns_batch *batch, const float *Lstar_dev, const uint32_t *keys_dev, void *stream);
 
 /* Standalone tree count and evidence statistics for one sample set (device pointers) */

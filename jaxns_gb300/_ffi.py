@@ -36,7 +36,7 @@ class EvCalc(ctypes.Structure):
 class RunDesc(ctypes.Structure):
     _fields_ = [("D", c_int), ("n", c_int), ("s", c_int), ("S", c_int), ("K", c_int), ("family", c_int),
                 ("midpoint", c_int), ("uniform_phase", c_int), ("N", c_int), ("pad0", c_int),
-                ("init_efficiency_threshold", c_double), ("cap", c_ll), ("live_off", c_ll),
+                ("init_efficiency_threshold", c_double), ("log_L_offset", c_double), ("cap", c_ll), ("live_off", c_ll),
                 ("store_off", c_ll), ("shell_off", c_ll), ("param_off", c_ll), ("prior_off", c_ll),
                 ("ustore_off", c_ll), ("liveU_off", c_ll), ("newU_off", c_ll), ("phU_off", c_ll),
                 ("phL_off", c_ll), ("tc", TermCond)]

@@ -58,10 +58,22 @@ __device__ __forceinline__ uint64_t bits64(Key k, uint32_t i) {
   return ((uint64_t)a << 32) | (uint64_t)b;
 }
 
+// Round-to-nearest-even conversion of a 64-bit unsigned integer to fp32 using 32-bit
+// operations only (a native 64-bit conversion runs on the FP64 pipe, which is scarce on
+// GB300): normalise, keep the top 32 bits with a sticky bit for the rest, convert, rescale.
+__device__ __forceinline__ float u64_to_float_rn(uint64_t x) {
+  if (x == 0ull) return 0.0f;
+  const int nz = __clzll(x);
+  const uint64_t y = x << nz;
+  const uint32_t top = (uint32_t)(y >> 32) | ((uint32_t)y != 0u ? 1u : 0u);
+  const float f = __uint2float_rn(top);                       // exact scale 2^(32 - nz) follows
+  return f * __int_as_float((127 + 32 - nz) << 23);           // 32 - nz in [-31, 32]
+}
+
 // jax.random.uniform(float64) in [0,1) from 64 bits: the top 52 bits M give M * 2^-52;
 // rounded once to fp32.
 __device__ __forceinline__ float uniform01(uint64_t b) {
-  return __ull2float_rn(b >> 12) * 2.220446049250313e-16f;  // 2^-52
+  return u64_to_float_rn(b >> 12) * 2.220446049250313e-16f;  // 2^-52
 }
 
 // jax.random.normal(float64) = sqrt(2) * erfinv(u) with u = 2f - 1 + 2^-53, f = M * 2^-52
@@ -72,10 +84,10 @@ __device__ __forceinline__ float normal_from_bits(uint64_t b) {
   const uint64_t M = b >> 12;
   if (M >= (1ull << 51)) {
     const uint64_t q = (1ull << 54) - 4ull * M - 1ull;  // (1 - u) * 2^53
-    return GBNS_SQRT2F * erfcinvf(__ull2float_rn(q) * 1.1102230246251565e-16f);
+    return GBNS_SQRT2F * erfcinvf(u64_to_float_rn(q) * 1.1102230246251565e-16f);
   } else {
     const uint64_t q = 4ull * M + 1ull;  // (1 + u) * 2^53
-    return -GBNS_SQRT2F * erfcinvf(__ull2float_rn(q) * 1.1102230246251565e-16f);
+    return -GBNS_SQRT2F * erfcinvf(u64_to_float_rn(q) * 1.1102230246251565e-16f);
   }
 }
 
@@ -244,6 +256,14 @@ __device__ __forceinline__ EvAcc evacc_from(const gbns_evcalc &e) {
   return a;
 }
 
+// As evacc_from for a register whose log_L is absolute while the scanned values are
+// relative to Loff.
+__device__ __forceinline__ EvAcc evacc_from_shifted(const gbns_evcalc &e, double Loff) {
+  EvAcc a = evacc_from(e);
+  a.Lprev = (float)(e.log_L - Loff);
+  return a;
+}
+
 __device__ __forceinline__ gbns_evcalc evacc_to(const EvAcc &a, double log_L_last) {
   gbns_evcalc e;
   e.log_L = log_L_last;
@@ -312,15 +332,17 @@ __device__ __forceinline__ void warp_lse_incl_scan(double v, double &q, int &e) 
 // Process elements [0, M) of log-likelihoods L (fp32) with live-point counts given by
 // nmode: nconst > 0 -> n_k = nconst; ndesc > 0 -> n_k = ndesc - k; else n_k = narr[k].
 // Must be called by all 32 lanes of one warp.  Optional per-element outputs (FP64 logs).
+// L values are relative to Loff (added back in FP64); Lidx, when given, gathers L[Lidx[k]].
 __device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ L, long long M, int nconst, int ndesc,
                                    const int *__restrict__ narr, const double *__restrict__ ncoef, int nmax,
                                    double *__restrict__ out_lX, double *__restrict__ out_ldZ,
-                                   double *__restrict__ out_lZ) {
+                                   double *__restrict__ out_lZ, double Loff = 0.0,
+                                   const int *__restrict__ Lidx = nullptr) {
   const int lane = threadIdx.x & 31;
   for (long long base = 0; base < M; base += 32) {
     const long long k = base + lane;
     const bool valid = k < M;
-    const float Lk = valid ? L[k] : 0.0f;
+    const float Lk = valid ? L[Lidx ? Lidx[k] : k] : 0.0f;
     float Lm1 = __shfl_up_sync(0xffffffffu, Lk, 1);
     if (lane == 0) Lm1 = acc.Lprev;
     int nk = 1;
@@ -338,7 +360,7 @@ __device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ 
     const double sT = warp_incl_scan(lT), sT2 = warp_incl_scan(lT2);
     const double lX_prev = acc.lX + (sT - lT), lX2_prev = acc.lX2 + (sT2 - lT2);
     const double lX_cur = acc.lX + sT;
-    const double lmid = valid ? log_midpoint(Lk, Lm1) : -INFINITY;
+    const double lmid = valid ? log_midpoint(Lk, Lm1) + Loff : -INFINITY;
     const double v_dZ = valid ? (lX_prev + lt) + lmid : -INFINITY;
     const double v_c = valid ? ((lX2_prev + ltT) + lmid) - lX_cur : -INFINITY;
     const double v_t2 = valid ? (lX2_prev + lt2) + 2.0 * lmid : -INFINITY;

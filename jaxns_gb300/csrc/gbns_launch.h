@@ -6,6 +6,7 @@
 namespace gbns {
 
 cudaError_t launch_slice_shells(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
+cudaError_t launch_slice_warp(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
 cudaError_t launch_init(const gbns_batch &b, long long total_points, cudaStream_t stream);
 cudaError_t launch_merge(const gbns_batch &b, cudaStream_t stream);
 cudaError_t launch_finalize(const gbns_batch &b, cudaStream_t stream);

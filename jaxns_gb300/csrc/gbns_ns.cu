@@ -11,7 +11,9 @@ namespace gbns {
 
 // ------------------------------------------------------ generic likelihood ----
 
-// Model.forward for any family with runtime D (parameters read from global memory).
+// Model.forward for any family with runtime D (parameters read from global memory),
+// relative to the run's log_L_offset: MVN -0.5 |Linv (x - mu)|^2, shells
+// logaddexp(-0.5 z1^2, -0.5 z2^2), linear Gaussian -0.5 |y - Phi w|^2 / sigma^2.
 __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, const float *U) {
   const int D = rd.D;
   const float *fp = b.fparams + rd.param_off;
@@ -27,7 +29,7 @@ __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, co
       for (int j = 0; j <= i; ++j) acc = fmaf(fp[D + i * D + j], x[j], acc);
       s = fmaf(acc, acc, s);
     }
-    v = fmaf(-0.5f, s, fp[D + D * D]);
+    v = -0.5f * s;
   } else if (rd.family == GBNS_LIK_SHELLS) {
     float r1 = 0.f, r2 = 0.f;
     for (int j = 0; j < D; ++j) {
@@ -35,9 +37,9 @@ __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, co
       r1 = fmaf(e1, e1, r1);
       r2 = fmaf(e2, e2, r2);
     }
-    const float R = fp[2 * D], w = fp[2 * D + 1], norm = fp[2 * D + 2];
+    const float R = fp[2 * D], w = fp[2 * D + 1];
     const float z1 = (sqrtf(r1) - R) / w, z2 = (sqrtf(r2) - R) / w;
-    const float s1 = fmaf(-0.5f * z1, z1, -norm), s2 = fmaf(-0.5f * z2, z2, -norm);
+    const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
     const float m = fmaxf(s1, s2), dd = s1 - s2;
     v = (dd != dd) ? s1 + s2 : m + log1pf(__expf(-fabsf(dd)));
   } else {
@@ -50,7 +52,7 @@ __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, co
       for (int j = 0; j < D; ++j) r = fmaf(-Phi[(size_t)a * D + j], x[j], r);
       ss = fmaf(r, r, ss);
     }
-    v = -0.5f * (float)N * logf(6.283185307179586f * sigma * sigma) - 0.5f * ss / (sigma * sigma);
+    v = -0.5f * ss / (sigma * sigma);
   }
   return (v != v) ? -INFINITY : v;
 }
@@ -59,7 +61,7 @@ __global__ void k_forward(gbns_batch b, int run, const float *__restrict__ U, fl
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= B) return;
   const gbns_run_desc &rd = b.runs[run];
-  out[i] = loglik_generic(b, rd, U + i * rd.D);
+  out[i] = (float)((double)loglik_generic(b, rd, U + i * rd.D) + rd.log_L_offset);
 }
 
 // ------------------------------------------------------------ termination ----
@@ -352,21 +354,22 @@ __global__ void __launch_bounds__(1024) k_merge(gbns_batch b) {
 
   // evidence register (sharded_static.py:284-299) by warp 0
   if (threadIdx.x < 32) {
-    EvAcc acc = evacc_from(st.ev);
-    evidence_scan_warp(acc, L, s, n, 0, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr);
-    const gbns_evcalc ev = evacc_to(acc, (double)L[s - 1]);
-    evidence_scan_warp(acc, oL, n, 0, n, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr);
-    const gbns_evcalc evr = evacc_to(acc, (double)oL[n - 1]);
+    const double off = rd.log_L_offset;
+    EvAcc acc = evacc_from_shifted(st.ev, off);
+    evidence_scan_warp(acc, L, s, n, 0, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr, off);
+    const gbns_evcalc ev = evacc_to(acc, (double)L[s - 1] + off);
+    evidence_scan_warp(acc, oL, n, 0, n, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr, off);
+    const gbns_evcalc evr = evacc_to(acc, (double)oL[n - 1] + off);
     if (threadIdx.x == 0) {
       st.ev = ev;
       st.ev_rem = evr;
       st.num_samples += (long long)s * (1 + K);
       st.next_sample_idx = nsi;
       st.num_likelihood_evaluations += sumNew;
-      st.log_L_contour = Lstar;
+      st.log_L_contour = (double)Lstar + off;
       st.efficiency = (double)n / (double)sumLive;
       st.plateau = flat;
-      const double Lmin = oL[0], Lmax = oL[n - 1];
+      const double Lmin = (double)oL[0] + off, Lmax = (double)oL[n - 1] + off;
       st.absolute_spread = fabs(Lmax - Lmin);
       st.relative_spread = 2.0 * st.absolute_spread / fabs(Lmin + Lmax);
       st.no_seed_points = oL[s - 1] >= oL[n - 1];

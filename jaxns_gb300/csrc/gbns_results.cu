@@ -169,12 +169,13 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
   cta_count_edges(b.store_S + so, N, perm, deg, si, nl, sm);
   __syncthreads();
   // gather in sorted order
-  float *Ls = res.log_L_samples + so;
+  double *Ls = res.log_L_samples + so;
+  const double off = rd.log_L_offset;
   int *Es = res.nevals_sorted + so;
   long long ev_sum = 0, ph_sum = 0;
   for (long long i = threadIdx.x; i < N; i += blockDim.x) {
     const int k = si[i];
-    Ls[i] = b.store_L[so + k];
+    Ls[i] = (double)b.store_L[so + k] + off;
     const int e = b.store_E[so + k];
     Es[i] = e;
     ev_sum += e;
@@ -198,7 +199,7 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
     e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
     e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
     EvAcc acc = evacc_from(e);
-    evidence_scan_warp(acc, Ls, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr);
+    evidence_scan_warp(acc, b.store_L + so, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr, off, si);
     if (threadIdx.x == 0) {
       const gbns_evcalc f = evacc_to(acc, 0.0);
       s_lz[0] = f.log_Z_mean;

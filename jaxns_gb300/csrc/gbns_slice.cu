@@ -48,7 +48,7 @@ __device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, cons
         s = fmaf(acc, acc, s);
       }
     }
-    v = fmaf(-0.5f, s, P.c0);
+    v = -0.5f * s;
   } else {
     float r1 = 0.0f, r2 = 0.0f;
 #pragma unroll
@@ -60,7 +60,7 @@ __device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, cons
       }
     }
     const float z1 = (sqrtf(r1) - P.R) / P.w, z2 = (sqrtf(r2) - P.R) / P.w;
-    const float s1 = fmaf(-0.5f * z1, z1, -P.norm), s2 = fmaf(-0.5f * z2, z2, -P.norm);
+    const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
     const float m = fmaxf(s1, s2), dd = s1 - s2;
     v = (dd != dd) ? s1 + s2 : m + log1pf(__expf(-fabsf(dd)));
   }
@@ -260,23 +260,26 @@ static cudaError_t launch_bucket(const gbns_batch &b, int fam, int ib, int ie, c
   const int nblk = ie - ib;
   if (nblk <= 0) return cudaSuccess;
   const int threads = b.chains_per_item;
-  if (fam == GBNS_LIK_MVN)
-    k_slice_shell<DMAX, GBNS_LIK_MVN><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
-  else
+  if (fam == GBNS_LIK_MVN) {
+    if (DMAX <= 16) k_slice_shell<(DMAX <= 16 ? DMAX : 16), GBNS_LIK_MVN><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+  } else {
     k_slice_shell<DMAX, GBNS_LIK_SHELLS><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+  }
   return cudaGetLastError();
 }
 
 // Buckets are (family, DMAX) pairs: bucket = fam * 4 + {0: D<=8, 1: D<=16, 2: D<=32, 3: D<=64}.
+// The correlated-Gaussian buckets with D > 16 run the warp-cooperative kernel
+// (gbns_slice_warp.cu); everything else runs one thread per chain here.
 cudaError_t launch_slice_shells(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream) {
-  for (int fam = 0; fam < 2; ++fam) {
-    cudaError_t e;
-    const int o = fam * 4;
-    if ((e = launch_bucket<8>(b, fam, b.bucket_begin[o + 0], b.bucket_end[o + 0], Lstar, keys, stream))) return e;
-    if ((e = launch_bucket<16>(b, fam, b.bucket_begin[o + 1], b.bucket_end[o + 1], Lstar, keys, stream))) return e;
-    if ((e = launch_bucket<32>(b, fam, b.bucket_begin[o + 2], b.bucket_end[o + 2], Lstar, keys, stream))) return e;
-    if ((e = launch_bucket<64>(b, fam, b.bucket_begin[o + 3], b.bucket_end[o + 3], Lstar, keys, stream))) return e;
-  }
+  cudaError_t e;
+  if ((e = launch_bucket<8>(b, 0, b.bucket_begin[0], b.bucket_end[0], Lstar, keys, stream))) return e;
+  if ((e = launch_bucket<16>(b, 0, b.bucket_begin[1], b.bucket_end[1], Lstar, keys, stream))) return e;
+  if ((e = launch_slice_warp(b, Lstar, keys, stream))) return e;
+  if ((e = launch_bucket<8>(b, 1, b.bucket_begin[4], b.bucket_end[4], Lstar, keys, stream))) return e;
+  if ((e = launch_bucket<16>(b, 1, b.bucket_begin[5], b.bucket_end[5], Lstar, keys, stream))) return e;
+  if ((e = launch_bucket<32>(b, 1, b.bucket_begin[6], b.bucket_end[6], Lstar, keys, stream))) return e;
+  if ((e = launch_bucket<64>(b, 1, b.bucket_begin[7], b.bucket_end[7], Lstar, keys, stream))) return e;
   return cudaSuccess;
 }
 

@@ -61,6 +61,7 @@ class RunSpec:
     init_efficiency_threshold: float = 0.1
     store_U: bool = True
     N: int = 0
+    log_L_offset: float = 0.0  # FP64 constant part of log L (device values are relative to it)
 
 
 def ncoef_table(nmax: int) -> np.ndarray:
@@ -115,7 +116,7 @@ class NSBatch:
     """Device state of R independent runs."""
 
     def __init__(self, specs: List[RunSpec], device="cuda", chains_per_item: int = 64,
-                 max_evals_per_slice: int = 100000):
+                 max_evals_per_slice: int = 100000, wide_chains_per_item: int = 0):
         if not specs:
             raise ValueError("no runs")
         self.specs = specs
@@ -158,6 +159,7 @@ class NSBatch:
             d.uniform_phase = int(s.init_efficiency_threshold > 0.0)
             d.N = s.N
             d.init_efficiency_threshold = float(s.init_efficiency_threshold)
+            d.log_L_offset = float(s.log_L_offset)
             d.cap = int(caps[r])
             d.live_off, d.store_off, d.shell_off = int(live_off[r]), int(store_off[r]), int(shell_off[r])
             d.param_off, d.prior_off, d.ustore_off = int(param_off[r]), int(prior_off[r]), int(ustore_off[r])
@@ -211,8 +213,14 @@ class NSBatch:
         items = []
         for r, s in enumerate(specs):
             b = s.family * 4 + _dbucket(s.D)
-            for c0 in range(0, s.shell_size, CH):
-                items.append((b, -s.D, r, c0, min(CH, s.shell_size - c0)))
+            # warp-cooperative buckets (MVN, D > 16): one chain per lane of the CTA (256 lanes
+            # for D > 32, 512 for 16 < D <= 32), so the lanes of a CTA finish together
+            if s.family != FAMILY_MVN or s.D <= 16:
+                ch = CH
+            else:
+                ch = int(wide_chains_per_item) if wide_chains_per_item else (256 if s.D > 32 else 512)
+            for c0 in range(0, s.shell_size, ch):
+                items.append((b, -s.D, r, c0, min(ch, s.shell_size - c0)))
         items.sort()
         arr = np.array([[it[2], it[3], it[4], 0] for it in items], np.int32).reshape(-1, 4)
         self.items = torch.from_numpy(arr).to(dev)
@@ -367,7 +375,7 @@ class NSBatch:
         R = self.R
         z = lambda n, dt: torch.zeros(n, dtype=dt, device=dev)
         out = dict(samples_indices=z(capsum, torch.int32), num_live_points=z(capsum, torch.int32),
-                   log_L_samples=z(capsum, torch.float32), log_dp_mean=z(capsum, torch.float64),
+                   log_L_samples=z(capsum, torch.float64), log_dp_mean=z(capsum, torch.float64),
                    log_X_mean=z(capsum, torch.float64), nevals_sorted=z(capsum, torch.int32),
                    scalars=z(R * 8, torch.float64))
         out["U_sorted"] = z(self.store_U.numel(), torch.float32) if (with_U and self.store_U is not None) else None
@@ -402,8 +410,9 @@ class NSBatch:
         s = self.specs[r]
         o = int(self.offsets["store"][r])
         N = int(min(st["num_samples"][r], s.max_samples))
-        d = dict(log_L=self.store_L[o:o + N], sender=self.store_S[o:o + N], nevals=self.store_E[o:o + N],
-                 phantom=self.store_P[o:o + N])
+        raw = self.store_L[o:o + N]
+        d = dict(log_L=raw.double() + s.log_L_offset, log_L_raw=raw, sender=self.store_S[o:o + N],
+                 nevals=self.store_E[o:o + N], phantom=self.store_P[o:o + N])
         if self.store_U is not None and self.offsets["ustore"][r] >= 0:
             uo = int(self.offsets["ustore"][r])
             d["U"] = self.store_U[uo:uo + N * s.D].view(N, s.D)
@@ -416,7 +425,8 @@ class NSBatch:
         o = int(self.offsets["live"][r])
         uo = int(self.offsets["liveU"][r])
         n = s.num_live_points
-        return dict(U=self.live_U[p][uo:uo + n * s.D].view(n, s.D), log_L=self.live_L[p][o:o + n],
+        raw = self.live_L[p][o:o + n]
+        return dict(U=self.live_U[p][uo:uo + n * s.D].view(n, s.D), log_L=raw.double() + s.log_L_offset, log_L_raw=raw,
                     nevals=self.live_E[p][o:o + n], sender=self.live_S[p][o:o + n],
                     log_L_constraint=self.live_Lc[p][o:o + n])
 
@@ -429,15 +439,17 @@ class NSBatch:
         return out
 
     def slice_shell(self, Lstar: torch.Tensor, keys: torch.Tensor):
-        """One shell of every run from the current live sets with explicit contours and
-        sample keys (test hook): outputs in new_U / new_L / new_E."""
+        """One shell of every run from the current live sets with explicit contours (relative
+        to each run's log_L_offset, like the device log-likelihoods) and sample keys (test
+        hook): outputs in new_U / new_L (relative) / new_E."""
         Lstar = Lstar.to(device=self.device, dtype=torch.float32).contiguous()
         keys = keys.to(device=self.device, dtype=torch.int32).contiguous()
         _ffi.call("gbns_slice_shell", ctypes.byref(self._b), ctypes.c_void_p(Lstar.data_ptr()),
                   ctypes.c_void_p(keys.data_ptr()), self._stream())
 
     def set_live(self, r: int, U: np.ndarray, log_L: np.ndarray):
-        """Overwrite run r's current live set (test hook; values must be sorted by log_L)."""
+        """Overwrite run r's current live set (test hook; values sorted, relative to the
+        run's log_L_offset)."""
         st = self.state()
         p = int(st["parity"][r])
         s = self.specs[r]
@@ -449,6 +461,16 @@ class NSBatch:
 
 
 # --------------------------------------------------------------- model tables
+
+def mvn_offset(cov) -> float:
+    """-sum log L_ii - D/2 log 2 pi: the constant of the Gaussian log density."""
+    L = np.linalg.cholesky(np.asarray(cov, np.float64))
+    return float(-np.sum(np.log(np.diag(L))) - 0.5 * L.shape[0] * np.log(2.0 * np.pi))
+
+
+def shells_offset(width) -> float:
+    return float(-np.log(np.sqrt(2.0 * np.pi * float(width) ** 2)))
+
 
 def mvn_params(mu, cov) -> np.ndarray:
     """[mu, Linv (row-major lower), c0] with L = chol(cov), c0 = -sum log L_ii - D/2 log 2 pi."""

@@ -8,7 +8,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .engine import FAMILY_LINGAUSS, FAMILY_MVN, FAMILY_SHELLS, mvn_params, shells_params
+from .engine import FAMILY_LINGAUSS, FAMILY_MVN, FAMILY_SHELLS, mvn_offset, mvn_params, shells_offset, shells_params
 
 
 class MultivariateNormalLikelihood:
@@ -26,6 +26,9 @@ class MultivariateNormalLikelihood:
 
     def params(self, model) -> np.ndarray:
         return mvn_params(self.mu, self.cov)
+
+    def log_L_offset(self) -> float:
+        return mvn_offset(self.cov)
 
     def __call__(self, x):
         x = np.asarray(x, np.float64)
@@ -50,6 +53,9 @@ class GaussianShellsLikelihood:
     def params(self, model) -> np.ndarray:
         return shells_params(self.c1, self.c2, self.radius, self.width)
 
+    def log_L_offset(self) -> float:
+        return shells_offset(self.width)
+
     def __call__(self, x):
         x = np.asarray(x, np.float64)
         norm = np.log(np.sqrt(2 * np.pi * self.width ** 2))
@@ -73,6 +79,9 @@ class LinearGaussianLikelihood:
 
     def params(self, model) -> np.ndarray:
         return np.concatenate([self.Phi.ravel(), self.y, [self.sigma]]).astype(np.float32)
+
+    def log_L_offset(self) -> float:
+        return float(-0.5 * len(self.y) * np.log(2.0 * np.pi * self.sigma ** 2))
 
     def __call__(self, w):
         r = self.y - np.asarray(w, np.float64) @ self.Phi.T

@@ -201,7 +201,8 @@ class ShardedStaticNestedSampler:
                        max_samples=self.max_samples, term_cond=term_cond.as_dict(), key=np.asarray(key, np.uint32),
                        num_phantom=self.sampler.num_phantom(), midpoint_shrink=self.sampler.midpoint_shrink,
                        init_efficiency_threshold=self.init_efficiency_threshold, store_U=self.store_U,
-                       N=int(getattr(m.log_likelihood, "Phi", np.zeros((0, 0))).shape[0]))
+                       N=int(getattr(m.log_likelihood, "Phi", np.zeros((0, 0))).shape[0]),
+                       log_L_offset=m.log_likelihood.log_L_offset())
 
     def _run(self, key, term_cond: TerminationCondition):
         batch = NSBatch([self.run_spec(key, term_cond)], device="cuda")
@@ -220,7 +221,7 @@ def results_from_batch(model: Model, batch: NSBatch, r: int, termination_reason:
     if U is not None:
         Ud = U.double()
         samples = model.transform(Ud)
-        lpd = v["log_L_samples"].double() + model.log_prob_prior(Ud)
+        lpd = v["log_L_samples"] + model.log_prob_prior(Ud)
     else:
         samples, lpd = {}, None
     return NestedSamplerResults(

@@ -66,11 +66,11 @@ def test_results_on_gpu_store_match_oracle(gpu_lib, oracle_mod):
     res = ns.to_results(reason, state)
     sc = state.sample_collection
     sender = sc.sender_node_idx.cpu().numpy()
-    L = sc.log_L.cpu().numpy().astype(np.float64)
+    L = sc.log_L.cpu().numpy()  # absolute log L (device fp32 + FP64 offset)
     si, nl = oracle_mod.count_crossed_edges(sender, L)
     np.testing.assert_array_equal(res.num_live_points_per_sample.cpu().numpy(), nl)
     ls = L[si]
-    np.testing.assert_array_equal(res.log_L_samples.cpu().numpy(), ls.astype(np.float32))
+    np.testing.assert_array_equal(res.log_L_samples.cpu().numpy(), ls)
     fin, per = oracle_mod.compute_evidence_stats(ls, nl.astype(np.float64))
     mu_o, var_o = oracle_mod.linear_to_log_stats(fin["log_Z_mean"], fin["log_Z2_mean"])
     assert abs(res.log_Z_mean - mu_o) < 1e-6
@@ -118,7 +118,7 @@ def test_graph_replay_equals_eager(gpu_lib):
 
 def test_batched_uneven_runs(gpu_lib):
     """Independent runs with different D, n and store sizes in one batch."""
-    from jaxns_gb300.engine import NSBatch, RunSpec, mvn_params
+    from jaxns_gb300.engine import NSBatch, RunSpec, mvn_offset, mvn_params
     specs = []
     Ds = [2, 3, 5, 8, 11, 16, 20, 33]
     for r, D in enumerate(Ds):
@@ -130,7 +130,7 @@ def test_batched_uneven_runs(gpu_lib):
                              params=mvn_params(mu, cov), prior_kind=np.zeros(D, np.int32),
                              prior_a=np.full(D, -10.0), prior_b=np.full(D, 20.0), max_samples=cap,
                              term_cond={"dlogZ": 1e-4, "max_samples": float(cap)},
-                             key=gb_key(r), store_U=False))
+                             key=gb_key(r), store_U=False, log_L_offset=mvn_offset(cov)))
     b = NSBatch(specs)
     st = b.run(block=8)
     out = b.results(with_U=False)

@@ -18,18 +18,21 @@ def _s():
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
 
-def _spec(D, n, S, seed_key, family=0, params=None, cap=None, tc=None, K=0, store_U=True, seed=0, low=-10., high=10.):
-    from jaxns_gb300.engine import RunSpec, mvn_params
+def _spec(D, n, S, seed_key, family=0, params=None, cap=None, tc=None, K=0, store_U=True, seed=0, low=-10., high=10.,
+          offset=None):
+    from jaxns_gb300.engine import RunSpec, mvn_offset, mvn_params
     mu, cov = corr_gauss(D, seed)
     if params is None:
         params = mvn_params(mu, cov)
+        offset = mvn_offset(cov)
     s = n // 2
     cap = cap or 100 * n
     cap = int(np.ceil(cap / (s * (1 + K))) * s * (1 + K))
     return RunSpec(D=D, num_live_points=n, shell_size=s, num_slices=S, family=family, params=params,
                    prior_kind=np.zeros(D, np.int32), prior_a=np.full(D, low), prior_b=np.full(D, high - low),
                    max_samples=cap, term_cond=dict(tc or {"dlogZ": 1e-4, "max_samples": float(cap)}),
-                   key=np.asarray(seed_key, np.uint32), num_phantom=K, store_U=store_U), (mu, cov)
+                   key=np.asarray(seed_key, np.uint32), num_phantom=K, store_U=store_U,
+                   log_L_offset=float(offset or 0.0)), (mu, cov)
 
 
 def test_rng_words_exact(gpu_lib, oracle_mod):
@@ -70,7 +73,7 @@ def test_uniform_normal_values(gpu_lib, oracle_mod):
 
 
 def test_forward_matches_oracle(gpu_lib, oracle_mod):
-    from jaxns_gb300.engine import NSBatch, shells_params
+    from jaxns_gb300.engine import NSBatch, shells_offset, shells_params
     for D in (2, 8, 13, 37, 64):
         spec, (mu, cov) = _spec(D, 64, D, oracle_mod.PRNGKey(0), seed=D)
         b = NSBatch([spec])
@@ -82,7 +85,8 @@ def test_forward_matches_oracle(gpu_lib, oracle_mod):
     D = 10
     c1 = np.zeros(D); c1[0] = 3.5
     c2 = -c1
-    spec, _ = _spec(D, 64, D, oracle_mod.PRNGKey(0), family=1, params=shells_params(c1, c2, 2.0, 0.1), low=-6., high=6.)
+    spec, _ = _spec(D, 64, D, oracle_mod.PRNGKey(0), family=1, params=shells_params(c1, c2, 2.0, 0.1), low=-6., high=6.,
+                    offset=shells_offset(0.1))
     b = NSBatch([spec])
     U = np.random.default_rng(0).uniform(0, 1, size=(300, D))
     U[:100] = (np.concatenate([[3.5 + 2.0], np.zeros(D - 1)]) + 6) / 12 + 0.01 * np.random.default_rng(1).standard_normal((100, D))
@@ -120,16 +124,17 @@ def test_slice_shell_chain_parity(gpu_lib, oracle_mod, D, n, S):
     b.init()
     live = b.live_view(0)
     s = n // 2
-    Lstar = float(live["log_L"][s - 1].item())
+    Lstar = float(live["log_L"][s - 1].item())          # absolute, for the oracle
+    Lstar_dev = float(live["log_L_raw"][s - 1].item())  # relative to the run's offset, for the device
     skey = oracle_mod.PRNGKey(1000 + D)
-    b.slice_shell(torch.tensor([Lstar]), torch.tensor(skey.view(np.int32)).view(1, 2))
+    b.slice_shell(torch.tensor([Lstar_dev]), torch.tensor(skey.view(np.int32)).view(1, 2))
     torch.cuda.synchronize()
     om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
     U_o, L_o, E_o = oracle_mod.slice_shell(om, skey, Lstar, live["U"].cpu().double().numpy(),
                                            live["log_L"].cpu().double().numpy(), s, S)
     E_g = b.new_E[:s].cpu().numpy()
     U_g = b.new_U[:s * D].view(s, D).cpu().numpy()
-    L_g = b.new_L[:s].cpu().numpy()
+    L_g = b.new_L[:s].cpu().double().numpy() + spec.log_L_offset
     same = (E_g == E_o) & np.all(np.abs(U_g - U_o) < 2e-4, axis=1)
     assert same.mean() >= 0.95, f"chain parity {same.mean():.3f}"
     np.testing.assert_allclose(L_g[same], L_o[same], rtol=1e-3, atol=1e-2)

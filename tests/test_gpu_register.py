@@ -1,0 +1,87 @@
+"""Per-iteration parity of the device termination register on the GPU's own sample stream:
+after every iteration, the oracle restatement of _collect_shell's register update
+(sharded_static.py:281-323) is applied to the GPU's discarded shell and sorted live set and
+compared with the device's FP64 register; the termination decision must agree."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+def _shells_batch(gb, key, n=1000, S=50):
+    from jaxns_gb300.engine import NSBatch
+    D = 10
+    c1 = np.zeros(D)
+    c1[0] = 3.5
+
+    def prior_model():
+        x = yield gb.Prior(gb.Uniform(-6.0 * np.ones(D), 6.0 * np.ones(D)), name="x")
+        return x
+
+    model = gb.Model(prior_model, gb.GaussianShellsLikelihood(c1, -c1, 2.0, 0.1))
+    ns = gb.NestedSampler(model, num_live_points=n, num_slices=S, max_samples=100000)
+    spec = ns.nested_sampler.run_spec(key, ns.normalise_term_cond(gb.TerminationCondition(dlogZ=1e-4)))
+    return NSBatch([spec]), model, c1
+
+
+def _ev(st):
+    return {k: float(st[k]) for k in ("log_L", "log_X_mean", "log_X2_mean", "log_Z_mean", "log_ZX_mean", "log_Z2_mean",
+                                      "log_dZ_mean", "log_dZ2_mean")}
+
+
+def test_register_replay_shells(gpu_lib, oracle_mod):
+    import jaxns_gb300 as gb
+    b, model, c1 = _shells_batch(gb, gb.random.PRNGKey(0))
+    b.init()
+    n, s = 1000, 500
+    for it in range(60):
+        st0 = b.state()[0]
+        if st0["done"]:
+            break
+        live0 = b.live_view(0)["log_L"].cpu().double().numpy()
+        b.iterate(1)
+        torch.cuda.synchronize()
+        st = b.state()[0]
+        live = b.live_view(0)["log_L"].cpu().double().numpy()
+        # discarded shell = the s lowest of the previous live set
+        ev = _ev(st0["ev"])
+        for L in live0[:s]:
+            ev = oracle_mod.evidence_update(ev, float(n), float(L))
+        evr = dict(ev)
+        for i, L in enumerate(live):
+            evr = oracle_mod.evidence_update(evr, float(n - i), float(L))
+        for f in ("log_X_mean", "log_Z_mean", "log_Z2_mean", "log_dZ2_mean", "log_ZX_mean"):
+            assert abs(st["ev"][f] - ev[f]) < 1e-6 * max(1, abs(ev[f])), (it, "ev", f, st["ev"][f], ev[f])
+            assert abs(st["ev_rem"][f] - evr[f]) < 1e-6 * max(1, abs(evr[f])), (it, "ev_rem", f, st["ev_rem"][f], evr[f])
+        reg = {"num_samples_used": int(st["num_samples"]), "ev": ev, "ev_rem": evr,
+               "num_likelihood_evaluations": int(st["num_likelihood_evaluations"]),
+               "log_L_contour": float(live0[s - 1]), "efficiency": float(st["efficiency"]),
+               "plateau": int(st["plateau"]), "no_seed_points": int(st["no_seed_points"]),
+               "relative_spread": float(st["relative_spread"]), "absolute_spread": float(st["absolute_spread"]),
+               "peak_log_XL": float(st["peak_log_XL"])}
+        done, reason = oracle_mod.determine_termination({"dlogZ": 1e-4, "max_samples": 100000 - s}, reg)
+        assert bool(st["done"]) == done, (it, done, reason)
+    assert 38 <= int(b.state()[0]["iterations"]) <= 46
+
+
+def test_shells_chain_parity(gpu_lib, oracle_mod):
+    import jaxns_gb300 as gb
+    b, model, c1 = _shells_batch(gb, gb.random.PRNGKey(1), n=200, S=50)
+    b.init()
+    for _ in range(6):  # move the contour into the shells
+        b.iterate(1)
+    torch.cuda.synchronize()
+    live = b.live_view(0)
+    s = 100
+    Lstar = float(live["log_L"][s - 1].item())
+    skey = gb.random.PRNGKey(77)
+    b.slice_shell(torch.tensor([float(live["log_L_raw"][s - 1].item())]), torch.tensor(skey.view(np.int32)).view(1, 2))
+    torch.cuda.synchronize()
+    om = oracle_mod.shells_model(-6, 6, c1, -c1, 2.0, 0.1)
+    U_o, L_o, E_o = oracle_mod.slice_shell(om, skey, Lstar, live["U"].cpu().double().numpy(),
+                                           live["log_L"].cpu().double().numpy(), s, 50)
+    E_g = b.new_E[:s].cpu().numpy()
+    U_g = b.new_U[:s * 10].view(s, 10).cpu().numpy()
+    same = (E_g == E_o) & np.all(np.abs(U_g - U_o) < 2e-4, axis=1)
+    assert same.mean() >= 0.95, f"chain parity {same.mean():.3f}"
