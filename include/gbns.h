@@ -223,6 +223,15 @@ int gbns_slice_shell(const gbns_batch *batch, const float *Lstar_dev, const uint
 /* Standalone tree count and evidence statistics for one sample set (device pointers) */
 int gbns_count_crossed_edges(const int *sender_dev, const float *log_L_dev, long long N, int *samples_indices_dev,
                              int *num_live_points_dev, long long *scratch_ll_dev, int *scratch_i_dev, void *stream);
+/* count_crossed_edges with no device allocation and no caller scratch, for callers that
+ * cannot call cudaMalloc (a host runtime that owns all device memory, such as an XLA FFI
+ * custom call; a real-time pipeline that cannot take cudaMalloc's implicit synchronisation;
+ * a deployment that forbids allocation after start-up).  No counterpart in the reference.
+ * Scratch is a file-scope device array (5 MiB per device, held until exit) shared by every
+ * call: N <= 262143, the first call on a device sets up its address (make it before any
+ * stream capture), and calls that overlap on the GPU race. */
+int gbns_count_crossed_edges_static(const int *sender_dev, const float *log_L_dev, long long N,
+                                    int *samples_indices_dev, int *num_live_points_dev, void *stream);
 int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,
                         int nmax, gbns_evcalc *final_dev, double *log_X_mean_dev, double *log_dZ_mean_dev,
                         double *log_Z_mean_dev, void *stream);

@@ -72,7 +72,8 @@ class ResultsBufs(ctypes.Structure):
 EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2x32", "gbns_threefry_split", "gbns_random_bits64",
             "gbns_uniform", "gbns_normal", "gbns_forward", "gbns_batch_init", "gbns_batch_iterate",
             "gbns_batch_finalize", "gbns_batch_results", "gbns_slice_shell", "gbns_count_crossed_edges",
-            "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event")
+            "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
+            "gbns_count_crossed_edges_static")
 
 _lib = None
 

@@ -32,6 +32,10 @@ int check_batch(const gbns_batch *b) {
 }
 }  // namespace
 
+namespace gbns {
+void record_error(const char *msg) { std::snprintf(g_err, sizeof(g_err), "%s", msg); }
+}  // namespace gbns
+
 extern "C" {
 
 int gbns_version(void) { return GBNS_VERSION; }

@@ -16,6 +16,8 @@ cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long l
                                        int *num_live, long long *scratch_ll, int *scratch_i, cudaStream_t stream);
 cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream);
+// Sets the thread-local message returned by gbns_last_error().
+void record_error(const char *msg);
 cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n,
                        cudaStream_t stream);
 
