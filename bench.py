@@ -207,6 +207,10 @@ def main():
     ap.add_argument("--block", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--only-dim", type=int, default=None,
+                    help="config3: keep only runs of this dimension (repeated to --runs); for kernel profiling")
+    ap.add_argument("--iterations", type=int, default=None,
+                    help="time init + this many NS iterations instead of whole runs (kernel profiling)")
     args = ap.parse_args()
     if args.runs is None:
         args.runs = 1024 if args.workload == "shells" else 4096
@@ -214,6 +218,11 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     wl = workload(args.runs, seed=2024 + rank, name=args.workload)
+    if args.only_dim is not None:
+        pool = [w for w in workload(4096, seed=2024 + rank, name=args.workload) if w[0] == args.only_dim]
+        if not pool:
+            raise SystemExit(f"no run of dimension {args.only_dim} in the workload")
+        wl = [pool[i % len(pool)] for i in range(args.runs)]
     threads = os.cpu_count() or 1
     if args.workload == "shells":
         wdesc = (f"configs[1] Gaussian shells D=10 (R=2, w=0.1, centres +-3.5 e0, U[-6,6]^10), 1000 live points, "
@@ -256,6 +265,22 @@ def main():
     keys = np.array([gb.random.PRNGKey(r) for r in range(len(wl))])
     bns = BatchedNestedSampler(samplers, keys, [gb.TerminationCondition(dlogZ=1e-4)] * len(wl), block=args.block)
     b = bns.batch
+    if args.iterations is not None:
+        # kernel-profiling mode: init + a fixed number of eager iterations, no results pass
+        b.init()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        b.iterate(args.iterations)
+        e1.record()
+        torch.cuda.synchronize()
+        st = b.state()
+        ev = int(st["num_likelihood_evaluations"].sum())
+        fl = float(np.sum(st["num_likelihood_evaluations"] * np.array([flops_per_eval(w[0], w[1]) for w in wl])))
+        ms = e0.elapsed_time(e1)
+        print(json.dumps({"mode": "iterations", "iterations": args.iterations, "runs": len(wl), "ms": ms,
+                          "likelihood_evals": ev, "algorithmic_tflops": fl / ms / 1e9}))
+        return
 
     def barrier():
         torch.cuda.synchronize()

@@ -67,23 +67,6 @@ __device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, cons
   return (v != v) ? -INFINITY : v;  // NaN -> -inf (framework/ops.py:323-325)
 }
 
-template <int DMAX>
-__device__ __forceinline__ void sample_direction(Key k, int D, float *d) {
-  if (D == 1) { d[0] = 1.0f; return; }
-  float s = 0.0f;
-#pragma unroll
-  for (int j = 0; j < DMAX; ++j) {
-    if (j < D) {
-      d[j] = normal_from_bits(bits64(k, (uint32_t)j));
-      s = fmaf(d[j], d[j], s);
-    }
-  }
-  const float nrm = sqrtf(s);
-#pragma unroll
-  for (int j = 0; j < DMAX; ++j)
-    if (j < D) d[j] = d[j] / nrm;
-}
-
 // linspace(0.5, 1, S)[j] as jnp.linspace evaluates it
 __device__ __forceinline__ float slice_alpha(int j, int S) {
   if (S == 1) return 0.5f;
@@ -141,8 +124,12 @@ __global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begi
   }
   __syncthreads();
 
-  const int c = c_begin + threadIdx.x;
-  if (threadIdx.x >= c_count) return;
+  // Every lane stays in the loop until its whole warp is done, so new directions can be
+  // generated warp-cooperatively; lanes past the item's chain count are idle from the start.
+  const bool valid = threadIdx.x < c_count;
+  const int c = c_begin + (valid ? threadIdx.x : 0);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __shared__ float dirbuf[4][32][DMAX + 1];
 
   // --- keys: _collect_shell split (sharded_static.py:248) then split(sample_key, s)[c]
   Key sample_key;
@@ -169,14 +156,18 @@ __global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begi
   }
   float u0[DMAX], d[DMAX];
 #pragma unroll
-  for (int j = 0; j < DMAX; ++j) u0[j] = (j < D) ? liveU[(size_t)idx * D + j] : 0.0f;
+  for (int j = 0; j < DMAX; ++j) {
+    u0[j] = (valid && j < D) ? liveU[(size_t)idx * D + j] : 0.0f;
+    d[j] = 0.0f;
+  }
   float logL0 = liveL[idx];
 
-  const Key direction_key = fold(chain_key, 0u), slices_key = fold(chain_key, 1u);
-  sample_direction<DMAX>(direction_key, D, d);
+  const Key slices_key = fold(chain_key, 1u);
+  Key dir_key = fold(chain_key, 0u);  // _sample_direction(direction_key) of get_sample_from_seed
+  bool need_dir = valid;
 
   // --- flattened slice / shrink loop
-  int j = 0;
+  int j = valid ? 0 : S;
   bool start = true;
   float left = 0.f, right = 0.f, t = 0.f, alpha = 0.5f;
   Key ck = {0u, 0u}, after_key = {0u, 0u};
@@ -186,13 +177,55 @@ __global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begi
   float *phU = b.ph_U + rd.phU_off + (size_t)c * K * D;
   float *phL = b.ph_L + rd.phL_off + (size_t)c * K;
   bool failed = false;
-  while (j < S) {
-    float u;
+  for (;;) {
+    // ---- new directions: the D normals of every lane that needs one, flattened over
+    // (lane, dimension) pairs across the warp
+    const unsigned dmask = __ballot_sync(0xffffffffu, need_dir);
+    if (dmask) {
+      if (D == 1) {
+        if (need_dir) d[0] = 1.0f;
+      } else {
+        const int cnt = __popc(dmask) * D;
+        for (int base = 0; base < cnt; base += 32) {
+          const int p = base + lane;
+          const bool ok = p < cnt;
+          const int src = ok ? (int)__fns(dmask, 0u, p / D + 1) : 0;
+          const Key dk = {__shfl_sync(0xffffffffu, dir_key.k0, src), __shfl_sync(0xffffffffu, dir_key.k1, src)};
+          if (ok) {
+            const int jj = p % D;
+            dirbuf[wid][src][jj] = normal_from_bits(bits64(dk, (uint32_t)jj));
+          }
+        }
+        __syncwarp();
+        if (need_dir) {
+          float ss = 0.0f;
+#pragma unroll
+          for (int q = 0; q < DMAX; ++q)
+            if (q < D) {
+              d[q] = dirbuf[wid][lane][q];
+              ss = fmaf(d[q], d[q], ss);
+            }
+          const float nrm = sqrtf(ss);
+#pragma unroll
+          for (int q = 0; q < DMAX; ++q)
+            if (q < D) d[q] = d[q] / nrm;
+        }
+        __syncwarp();
+      }
+      need_dir = false;
+    }
+    const bool active = j < S;
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (!active) continue;
+
+    // ---- one proposal: the first pick of slice j, or one shrink step (_new_proposal)
+    Key B;
+    if (start) B = fold(slices_key, (uint32_t)j);
+    else B = ck;
+    ck = fold(B, 0u);                              // run_key / next carry key
+    const Key tk = fold(B, start ? 2u : 1u);       // t_key
     if (start) {
-      const Key kj = fold(slices_key, (uint32_t)j);
-      ck = fold(kj, 0u);
-      const Key t_key = fold(kj, 2u);
-      after_key = fold(kj, 3u);
+      after_key = fold(B, 3u);
       alpha = slice_alpha(j, S);
       // _slice_bounds (uni_slice_sampler.py:41-64)
       float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
@@ -209,10 +242,8 @@ __global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begi
       }
       right = fminf(t0r, t1r);
       left = fmaxf(t0l, t1l);
-      u = uniform01(bits64(t_key, 0u));
       in_slice = 0;
     } else {
-      const Key nk = fold(ck, 0u), tk = fold(ck, 1u);
       // _shrink_interval (uni_slice_sampler.py:92-111)
       if (t < 0.f) left = t;
       if (t > 0.f) right = t;
@@ -220,9 +251,8 @@ __global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begi
         if (t < 0.f) left = alpha * left;
         if (t > 0.f) right = alpha * right;
       }
-      u = uniform01(bits64(tk, 0u));
-      ck = nk;
     }
+    const float u = uniform01(bits64(tk, 0u));
     // _pick_point_in_interval (uni_slice_sampler.py:67-89)
     t = fmaf(u, right - left, left);
     const float logL = loglik<DMAX, FAM>(P, D, u0, d, t);
@@ -242,11 +272,15 @@ __global__ void __launch_bounds__(128) k_slice_shell(gbns_batch b, int item_begi
       }
       ++j;
       start = true;
-      if (j < S) sample_direction<DMAX>(after_key, D, d);
+      if (j < S) {
+        need_dir = true;
+        dir_key = after_key;
+      }
     } else {
       start = false;
     }
   }
+  if (!valid) return;
   float *nu = b.new_U + rd.newU_off + (size_t)c * D;
   for (int q = 0; q < D; ++q) nu[q] = u0[q];
   b.new_L[out] = logL0;
