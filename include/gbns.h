@@ -165,6 +165,24 @@ typedef struct {
     int max_evals_per_slice;        /* shrink-loop evaluation budget per slice */
 } gbns_batch;
 
+/* Lock-step chain state of the linear-Gaussian family (device, caller-allocated).  Its
+ * likelihood is one dense contraction over all proposals of a step, so the slice sampler
+ * runs as alternating launches: gbns_lg_step (slice logic + next proposal per chain) and a
+ * batched residual kernel (|y - Phi w|^2 for every pending proposal).  Per-chain arrays are
+ * indexed like the shell outputs ([sum s] and [sum s * D]). */
+typedef struct {
+    int *j, *in_slice, *total, *flags;      /* [sum s] */
+    float *left, *right, *t, *alpha, *logL0; /* [sum s] */
+    uint32_t *ck, *after_key, *slices_key, *dir_key; /* [sum s * 2] */
+    float *u0, *dir, *W;                    /* [sum s * D]: seed point, direction, proposal w */
+    double *ss;                             /* [sum s] residual sums of the pending proposals */
+    int *chains_left;                       /* [R] chains of the current shell not yet finished */
+    const int *items;                       /* [num_items * 4]: (run, first chain, chain count, first data row) */
+    int num_items;
+    int pmax;                               /* largest D (= P) over the runs, <= 64 */
+    long long total_chains;                 /* sum of s over the runs */
+} gbns_lg_bufs;
+
 /* results buffers (device) */
 typedef struct {
     int *samples_indices;           /* [sum cap] */
@@ -232,6 +250,22 @@ int gbns_count_crossed_edges(const int *sender_dev, const float *log_L_dev, long
  * stream capture), and calls that overlap on the GPU race. */
 int gbns_count_crossed_edges_static(const int *sender_dev, const float *log_L_dev, long long N,
                                     int *samples_indices_dev, int *num_live_points_dev, void *stream);
+/* Linear-Gaussian family: start a shell for every active run (seed points, keys), then
+ * advance every chain num_steps likelihood evaluations (graph-capturable).  When every
+ * run's chains_left is 0, gbns_batch_merge completes the iteration.
+ *   <- get_samples / UniDimSliceSampler.get_sample (sharded_static.py:88-129,
+ *      uni_slice_sampler.py:343-441) for a likelihood evaluated in batches */
+int gbns_lg_shell_begin(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
+int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps, void *stream);
+
+/* Reweighted fixed-dead-point evidence of the linear-Gaussian model and its gradient
+ * (experimental/evidence_maximisation.py:151-160, weights :213):
+ *   log Z(theta) = logsumexp_i(log L_theta(U_i) + log_w_i),  w_i = tau * ndtri(U_i),
+ *   out[0] = log Z(theta), out[1] = d/d log tau, out[2] = d/d log sigma  (FP64 reductions).
+ * Per-point residuals are recomputed from U, never stored.  ss_scratch, ry_scratch: [M]. */
+int gbns_evidence_adjoint(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+                          const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
+                          double *ss_scratch_dev, double *ry_scratch_dev, void *stream);
 int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,
                         int nmax, gbns_evcalc *final_dev, double *log_X_mean_dev, double *log_dZ_mean_dev,
                         double *log_Z_mean_dev, void *stream);

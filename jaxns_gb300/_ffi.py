@@ -63,6 +63,14 @@ class Batch(ctypes.Structure):
                 ("chains_per_item", c_int), ("max_evals_per_slice", c_int)]
 
 
+class LGBufs(ctypes.Structure):
+    _fields_ = [("j", c_void_p), ("in_slice", c_void_p), ("total", c_void_p), ("flags", c_void_p),
+                ("left", c_void_p), ("right", c_void_p), ("t", c_void_p), ("alpha", c_void_p), ("logL0", c_void_p),
+                ("ck", c_void_p), ("after_key", c_void_p), ("slices_key", c_void_p), ("dir_key", c_void_p),
+                ("u0", c_void_p), ("dir", c_void_p), ("W", c_void_p), ("ss", c_void_p), ("chains_left", c_void_p),
+                ("items", c_void_p), ("num_items", c_int), ("pmax", c_int), ("total_chains", c_ll)]
+
+
 class ResultsBufs(ctypes.Structure):
     _fields_ = [("samples_indices", c_void_p), ("num_live_points", c_void_p), ("log_L_samples", c_void_p),
                 ("log_dp_mean", c_void_p), ("log_X_mean", c_void_p), ("nevals_sorted", c_void_p),
@@ -73,7 +81,7 @@ EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2
             "gbns_uniform", "gbns_normal", "gbns_forward", "gbns_batch_init", "gbns_batch_iterate",
             "gbns_batch_finalize", "gbns_batch_results", "gbns_slice_shell", "gbns_count_crossed_edges",
             "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
-            "gbns_count_crossed_edges_static")
+            "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint")
 
 _lib = None
 

@@ -1,0 +1,98 @@
+"""Evidence gradient of the linear-Gaussian model by reweighting a fixed dead-point set.
+
+EvidenceMaximisation (experimental/evidence_maximisation.py:151-160, weights :213) fixes the
+dead points U_i of one nested-sampling run and maximises
+    log Z(theta) = logsumexp_i(log L_theta(U_i) + log w_i),
+    log w_i = log_dp_mean_i - log L_i + log Z_mean,
+over the hyperparameters theta = (log tau, log sigma) of y ~ N(Phi w, sigma^2 I),
+w = tau * ndtri(U).  gbns_evidence_adjoint returns log Z(theta) and its exact gradient
+sum_i softmax_i * d log L_theta(U_i) / d theta, recomputing each point's residual from U.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _ffi
+
+
+@dataclass
+class DeadSet:
+    """The fixed dead points of one run (device tensors)."""
+    U: torch.Tensor        # [M, P] float32
+    log_w: torch.Tensor    # [M] float64
+    Phi: torch.Tensor      # [N, P] float32
+    y: torch.Tensor        # [N] float32
+
+    @staticmethod
+    def from_results(results, Phi, y) -> "DeadSet":
+        log_w = (results.log_dp_mean - results.log_L_samples + results.log_Z_mean).contiguous()
+        dev = results.U_samples.device
+        return DeadSet(U=results.U_samples.contiguous(), log_w=log_w.to(torch.float64),
+                       Phi=torch.as_tensor(np.asarray(Phi, np.float32), device=dev).contiguous(),
+                       y=torch.as_tensor(np.asarray(y, np.float32), device=dev).contiguous())
+
+
+def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float):
+    """(log Z(theta), d log Z / d log tau, d log Z / d log sigma) on the device, FP64."""
+    M, P = ds.U.shape
+    N = ds.Phi.shape[0]
+    dev = ds.U.device
+    out = torch.zeros(3, dtype=torch.float64, device=dev)
+    ss = torch.empty(max(M, 1), dtype=torch.float64, device=dev)
+    ry = torch.empty(max(M, 1), dtype=torch.float64, device=dev)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    _ffi.call("gbns_evidence_adjoint", p(ds.U), p(ds.log_w), ctypes.c_longlong(M), ctypes.c_int(P), p(ds.Phi),
+              p(ds.y), ctypes.c_int(N), ctypes.c_double(float(log_tau)), ctypes.c_double(float(log_sigma)), p(out),
+              p(ss), p(ry), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return out
+
+
+class EvidenceFn(torch.autograd.Function):
+    """log Z(theta) of a fixed dead set as a differentiable function of theta = (log tau, log sigma).
+    The backward pass recomputes the per-point likelihood gradients (nothing per point is
+    stored by the forward pass)."""
+
+    @staticmethod
+    def forward(ctx, theta: torch.Tensor, ds: DeadSet):
+        th = theta.detach().to(torch.float64).cpu().numpy()
+        out = evidence_and_grad(ds, th[0], th[1])
+        ctx.ds = ds
+        ctx.save_for_backward(theta)
+        return out[0].to(device=theta.device, dtype=theta.dtype)
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        (theta,) = ctx.saved_tensors
+        th = theta.detach().to(torch.float64).cpu().numpy()
+        out = evidence_and_grad(ctx.ds, th[0], th[1])
+        g = out[1:].to(device=theta.device, dtype=theta.dtype)
+        return grad_out.to(theta.device) * g, None
+
+
+def blr_log_evidence(Phi, y, log_tau, log_sigma):
+    """Analytic log N(y; 0, sigma^2 I + tau^2 Phi Phi^T) and its gradient in (log tau, log sigma),
+    FP64 (Woodbury / matrix-determinant lemma)."""
+    Phi = np.asarray(Phi, np.float64)
+    y = np.asarray(y, np.float64)
+    N, P = Phi.shape
+    t2, s2 = np.exp(2 * log_tau), np.exp(2 * log_sigma)
+    A = np.eye(P) / t2 + Phi.T @ Phi / s2           # P x P
+    L = np.linalg.cholesky(A)
+    Pty = Phi.T @ y
+    b = np.linalg.solve(A, Pty)
+    alpha = y / s2 - Phi @ b / s2 ** 2                # C^{-1} y
+    logdetC = N * np.log(s2) + P * np.log(t2) + 2 * np.sum(np.log(np.diag(L)))
+    logZ = -0.5 * (N * np.log(2 * np.pi) + logdetC + y @ alpha)
+    # d/dtheta: 0.5 (alpha^T dC alpha - tr(C^{-1} dC));  dC/dlog sigma = 2 s2 I, dC/dlog tau = 2 t2 Phi Phi^T
+    Ainv = np.linalg.inv(A)
+    trCinv = N / s2 - np.trace(Ainv @ (Phi.T @ Phi)) / s2 ** 2
+    PtP = Phi.T @ Phi
+    trCinvPP = np.trace(PtP) / s2 - np.trace(Ainv @ PtP @ PtP) / s2 ** 2
+    Pa = Phi.T @ alpha
+    g_sigma = 0.5 * (2 * s2 * (alpha @ alpha) - 2 * s2 * trCinv)
+    g_tau = 0.5 * (2 * t2 * (Pa @ Pa) - 2 * t2 * trCinvPP)
+    return logZ, np.array([g_tau, g_sigma])

@@ -1,0 +1,428 @@
+// gbns_phiw.cu -- the linear-Gaussian (Phi w) family: lock-step slice sampling with a
+// batched residual contraction, and the reweighted-evidence adjoint.
+//
+// log L(w) = -N/2 log(2 pi sigma^2) - |y - Phi w|^2 / (2 sigma^2), w = tau * ndtri(U) (the
+// Normal(0, tau^2) prior quantile).  One likelihood is an N x P contraction, so the chains of
+// a shell advance together: gbns_lg_step runs each chain's slice logic up to its next
+// proposal (same RNG stream and decisions as uni_slice_sampler.py:114-273, :343-441), and the
+// residual kernel evaluates |y - Phi w|^2 for all proposals of the step at once.
+#include <cstdio>
+#include "gbns_device.cuh"
+#include "gbns_launch.h"
+
+namespace gbns {
+
+enum : int { LG_START = 1, LG_NEED_DIR = 2, LG_PENDING = 4, LG_FAILED = 8, LG_DONE = 16 };
+
+__device__ __forceinline__ int run_of_chain(const gbns_batch &b, long long g) {
+  int lo = 0, hi = b.num_runs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (b.runs[mid].shell_off <= g) lo = mid; else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ float lg_alpha(int j, int S) {
+  if (S == 1) return 0.5f;
+  if (j == S - 1) return 1.0f;
+  const float step = (float)j / (float)(S - 1);
+  return 0.5f * (1.0f - step) + step;
+}
+
+// A chain's first state of the shell: seed point (resample_indicies over log L > L*),
+// direction and slice keys (get_sample_from_seed, uni_slice_sampler.py:403-423).
+__global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= total_chains) return;
+  const int r = run_of_chain(b, g);
+  const gbns_run_desc &rd = b.runs[r];
+  const gbns_run_state &st = b.state[r];
+  if (rd.family != GBNS_LIK_LINGAUSS || st.done || st.phase != 1) return;
+  const int c = (int)(g - rd.shell_off);
+  if (c >= rd.s) return;
+  const int n = rd.n, P = rd.D;
+  const float *liveL = b.live_L[st.parity] + rd.live_off;
+  const float *liveU = b.live_U[st.parity] + rd.liveU_off;
+  const float Lstar = liveL[rd.s - 1];
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (liveL[mid] > Lstar) hi = mid; else lo = mid + 1;
+  }
+  const int m = n - lo;
+  const Key k0 = {st.key[0], st.key[1]};
+  const Key sample_key = fold(fold(k0, 0u), 1u);
+  const Key kc = fold(sample_key, (uint32_t)c);
+  const Key chain_key = fold(kc, 0u), seed_key = fold(kc, 1u);
+  int idx = 0;
+  if (m > 0) {
+    const uint64_t M52 = bits64(seed_key, 0u) >> 12;
+    const uint64_t q = (1ull << 52) - M52;
+    const uint64_t lo64 = (uint64_t)m * q, hi64 = __umul64hi((uint64_t)m, q);
+    uint64_t kk = (hi64 << 12) | (lo64 >> 52);
+    if (lo64 & ((1ull << 52) - 1)) kk += 1;
+    idx = (n - m) + (int)kk - 1;
+  }
+  float *u0 = lg.u0 + rd.newU_off + (size_t)c * P;
+  for (int p = 0; p < P; ++p) u0[p] = liveU[(size_t)idx * P + p];
+  lg.logL0[g] = liveL[idx];
+  const Key dk = fold(chain_key, 0u), sk = fold(chain_key, 1u);
+  lg.dir_key[2 * g] = dk.k0;
+  lg.dir_key[2 * g + 1] = dk.k1;
+  lg.slices_key[2 * g] = sk.k0;
+  lg.slices_key[2 * g + 1] = sk.k1;
+  lg.flags[g] = LG_START | LG_NEED_DIR;
+  lg.j[g] = 0;
+  lg.total[g] = 0;
+  lg.in_slice[g] = 0;
+  lg.ss[g] = 0.0;
+  if (c == 0) lg.chains_left[r] = rd.s;
+}
+
+// One likelihood evaluation per chain: consume the pending result, then prepare the next
+// proposal w (written to lg.W) or finish the chain.
+__global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains) {
+  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (g >= total_chains) return;
+  const int r = run_of_chain(b, g);
+  const gbns_run_desc &rd = b.runs[r];
+  gbns_run_state &st = b.state[r];
+  if (rd.family != GBNS_LIK_LINGAUSS || st.done || st.phase != 1) return;
+  const int c = (int)(g - rd.shell_off);
+  if (c >= rd.s) return;
+  int flags = lg.flags[g];
+  if (flags & LG_DONE) return;
+  const int P = rd.D, S = rd.S, K = rd.K, N = rd.N;
+  const float *fp = b.fparams + rd.param_off;
+  const float sigma = fp[(size_t)N * P + N];
+  const float inv2s2 = 0.5f / (sigma * sigma);
+  const float Lstar = b.live_L[st.parity][rd.live_off + rd.s - 1];
+  float *u0 = lg.u0 + rd.newU_off + (size_t)c * P;
+  float *d = lg.dir + rd.newU_off + (size_t)c * P;
+  float *W = lg.W + rd.newU_off + (size_t)c * P;
+  int j = lg.j[g], total = lg.total[g], in_slice = lg.in_slice[g];
+  float left = lg.left[g], right = lg.right[g], t = lg.t[g], alpha = lg.alpha[g], logL0 = lg.logL0[g];
+  Key ck = {lg.ck[2 * g], lg.ck[2 * g + 1]};
+  Key after_key = {lg.after_key[2 * g], lg.after_key[2 * g + 1]};
+  Key dir_key = {lg.dir_key[2 * g], lg.dir_key[2 * g + 1]};
+  const Key slices_key = {lg.slices_key[2 * g], lg.slices_key[2 * g + 1]};
+
+  if (flags & LG_PENDING) {
+    const double ss = lg.ss[g];
+    lg.ss[g] = 0.0;
+    float logL = (float)(-ss * (double)inv2s2);  // relative to the run's log_L_offset
+    if (logL != logL) logL = -INFINITY;
+    ++total;
+    ++in_slice;
+    const bool accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
+    if (accept || in_slice >= b.max_evals_per_slice) {
+      if (!accept) flags |= LG_FAILED;
+      for (int p = 0; p < P; ++p) u0[p] = fmaf(t, d[p], u0[p]);
+      logL0 = logL;
+      const int ph = j - (S - 1 - K);
+      if (K > 0 && ph >= 0 && j < S - 1) {
+        float *phU = b.ph_U + rd.phU_off + ((size_t)c * K + ph) * P;
+        for (int p = 0; p < P; ++p) phU[p] = u0[p];
+        b.ph_L[rd.phL_off + (size_t)c * K + ph] = logL;
+      }
+      ++j;
+      flags |= LG_START;
+      if (j < S) {
+        flags |= LG_NEED_DIR;
+        dir_key = after_key;
+      } else {
+        flags |= LG_DONE;
+      }
+    } else {
+      flags &= ~LG_START;
+    }
+    flags &= ~LG_PENDING;
+  }
+  if (flags & LG_DONE) {
+    float *nu = b.new_U + rd.newU_off + (size_t)c * P;
+    for (int p = 0; p < P; ++p) nu[p] = u0[p];
+    b.new_L[rd.shell_off + c] = logL0;
+    b.new_E[rd.shell_off + c] = total;
+    if (flags & LG_FAILED) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
+    atomicSub(&lg.chains_left[r], 1);
+  } else {
+    if (flags & LG_NEED_DIR) {
+      if (P == 1) {
+        d[0] = 1.0f;
+      } else {
+        float ssd = 0.0f;
+        for (int p = 0; p < P; ++p) {
+          const float v = normal_from_bits(bits64(dir_key, (uint32_t)p));
+          d[p] = v;
+          ssd = fmaf(v, v, ssd);
+        }
+        const float nrm = sqrtf(ssd);
+        for (int p = 0; p < P; ++p) d[p] = d[p] / nrm;
+      }
+      flags &= ~LG_NEED_DIR;
+    }
+    const bool start = (flags & LG_START) != 0;
+    const Key B = start ? fold(slices_key, (uint32_t)j) : ck;
+    ck = fold(B, 0u);
+    const Key tk = fold(B, start ? 2u : 1u);
+    if (start) {
+      after_key = fold(B, 3u);
+      alpha = lg_alpha(j, S);
+      float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
+      for (int p = 0; p < P; ++p) {
+        const float t1 = (1.0f - u0[p]) / d[p], t0 = -u0[p] / d[p];
+        t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
+        t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
+        t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
+        t0l = fmaxf(t0l, t0 <= 0.f ? t0 : -INFINITY);
+      }
+      right = fminf(t0r, t1r);
+      left = fmaxf(t0l, t1l);
+      in_slice = 0;
+    } else {
+      if (t < 0.f) left = t;
+      if (t > 0.f) right = t;
+      if (rd.midpoint) {
+        if (t < 0.f) left = alpha * left;
+        if (t > 0.f) right = alpha * right;
+      }
+    }
+    t = fmaf(uniform01(bits64(tk, 0u)), right - left, left);
+    const int *kind = b.prior_kind + rd.prior_off;
+    const float *pa = b.prior_a + rd.prior_off, *pb = b.prior_b + rd.prior_off;
+    for (int p = 0; p < P; ++p) W[p] = prior_quantile(kind[p], pa[p], pb[p], fmaf(t, d[p], u0[p]));
+    flags |= LG_PENDING;
+  }
+  lg.flags[g] = flags;
+  lg.j[g] = j;
+  lg.total[g] = total;
+  lg.in_slice[g] = in_slice;
+  lg.left[g] = left;
+  lg.right[g] = right;
+  lg.t[g] = t;
+  lg.alpha[g] = alpha;
+  lg.logL0[g] = logL0;
+  lg.ck[2 * g] = ck.k0;
+  lg.ck[2 * g + 1] = ck.k1;
+  lg.after_key[2 * g] = after_key.k0;
+  lg.after_key[2 * g + 1] = after_key.k1;
+  lg.dir_key[2 * g] = dir_key.k0;
+  lg.dir_key[2 * g + 1] = dir_key.k1;
+}
+
+// |y - Phi w|^2 (and y . (y - Phi w)) for a 64-point x 64-row tile; FP64 atomics per point.
+// Points are rows of W (the pending proposals, or the dead set for the adjoint); in adjoint
+// mode W comes from U: w = tau * ndtri(u).
+template <int PMAX>
+__device__ __forceinline__ void resid_tile(const float *__restrict__ Wsrc, bool from_U, float tau, int npts, int P,
+                                           const float *__restrict__ Phi, const float *__restrict__ y, int N,
+                                           int row0, double *ss_out, double *ry_out) {
+  __shared__ float Ws[64][PMAX + 1];
+  __shared__ float Ps[64][PMAX + 1];
+  __shared__ float ys[64];
+  __shared__ float red_ss[16][65];
+  __shared__ float red_ry[16][65];
+  const int tid = threadIdx.x;
+  for (int q = tid; q < 64 * PMAX; q += blockDim.x) {
+    const int i = q / PMAX, k = q % PMAX;
+    float w = 0.0f;
+    if (i < npts && k < P) {
+      const float v = Wsrc[(size_t)i * P + k];
+      w = from_U ? tau * (GBNS_SQRT2F * erfinvf(fmaf(2.0f, v, -1.0f))) : v;
+    }
+    Ws[i][k] = w;
+    const int row = row0 + i;
+    Ps[i][k] = (row < N && k < P) ? Phi[(size_t)row * P + k] : 0.0f;
+  }
+  if (tid < 64) ys[tid] = (row0 + tid < N) ? y[row0 + tid] : 0.0f;
+  __syncthreads();
+  const int tx = tid & 15, ty = tid >> 4;
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+#pragma unroll 4
+  for (int k = 0; k < P; ++k) {
+    float wv[4], pv[4];
+#pragma unroll
+    for (int c = 0; c < 4; ++c) wv[c] = Ws[4 * tx + c][k];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) pv[a] = Ps[4 * ty + a][k];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[a][c] = fmaf(pv[a], wv[c], acc[a][c]);
+  }
+  float pss[4] = {0.f, 0.f, 0.f, 0.f}, pry[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    if (row0 + 4 * ty + a < N) {
+      const float yy = ys[4 * ty + a];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const float rr = yy - acc[a][c];
+        pss[c] = fmaf(rr, rr, pss[c]);
+        pry[c] = fmaf(rr, yy, pry[c]);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 4; ++c) {
+    red_ss[ty][4 * tx + c] = pss[c];
+    red_ry[ty][4 * tx + c] = pry[c];
+  }
+  __syncthreads();
+  if (tid < 64 && tid < npts) {
+    double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+    for (int q = 0; q < 16; ++q) {
+      s1 += (double)red_ss[q][tid];
+      s2 += (double)red_ry[q][tid];
+    }
+    atomicAdd(&ss_out[tid], s1);
+    if (ry_out) atomicAdd(&ry_out[tid], s2);
+  }
+}
+
+template <int PMAX>
+__global__ void __launch_bounds__(256) k_lg_resid(gbns_batch b, gbns_lg_bufs lg) {
+  const int *it = lg.items + 4 * (size_t)blockIdx.x;
+  const int r = it[0], c0 = it[1], nc = it[2], row0 = it[3];
+  const gbns_run_desc &rd = b.runs[r];
+  const gbns_run_state &st = b.state[r];
+  if (st.done || st.phase != 1) return;
+  const int P = rd.D, N = rd.N;
+  const float *fp = b.fparams + rd.param_off;
+  resid_tile<PMAX>(lg.W + rd.newU_off + (size_t)c0 * P, false, 0.0f, nc, P, fp, fp + (size_t)N * P, N, row0,
+                   lg.ss + rd.shell_off + c0, nullptr);
+}
+
+template <int PMAX>
+__global__ void __launch_bounds__(256) k_adj_resid(const float *U, long long M, int P, const float *Phi, const float *y,
+                                                   int N, float tau, double *ss, double *ry) {
+  const long long p0 = (long long)blockIdx.x * 64;
+  const int row0 = blockIdx.y * 64;
+  const int npts = (int)min(64ll, M - p0);
+  resid_tile<PMAX>(U + p0 * P, true, tau, npts, P, Phi, y, N, row0, ss + p0, ry + p0);
+}
+
+// log Z(theta) = logsumexp_i a_i, a_i = log L_theta(U_i) + log w_i, and its gradient
+// sum_i softmax(a)_i dlogL_i/dtheta, all in FP64.
+__global__ void __launch_bounds__(1024) k_adj_reduce(const double *log_w, long long M, int N, double log_sigma,
+                                                     const double *ss, const double *ry, double *out) {
+  __shared__ double red[32];
+  const double s2 = exp(2.0 * log_sigma);
+  const double c = -0.5 * (double)N * (log(2.0 * 3.141592653589793) + 2.0 * log_sigma);
+  double mx = -INFINITY;
+  for (long long i = threadIdx.x; i < M; i += blockDim.x) mx = fmax(mx, c - 0.5 * ss[i] / s2 + log_w[i]);
+  // max over the CTA
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = -INFINITY;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) mx = fmax(mx, red[q]);
+  __syncthreads();
+  double se = 0.0, gt = 0.0, gs = 0.0;
+  if (mx > -INFINITY) {
+    for (long long i = threadIdx.x; i < M; i += blockDim.x) {
+      const double a = c - 0.5 * ss[i] / s2 + log_w[i];
+      const double e = exp(a - mx);
+      se += e;
+      gt += e * ((ry[i] - ss[i]) / s2);   // r . (Phi w) / sigma^2
+      gs += e * (ss[i] / s2 - (double)N);  // |r|^2 / sigma^2 - N
+    }
+  }
+  se = cta_sum_d(se, red);
+  gt = cta_sum_d(gt, red);
+  gs = cta_sum_d(gs, red);
+  if (threadIdx.x == 0) {
+    out[0] = (mx > -INFINITY) ? mx + log(se) : -INFINITY;
+    out[1] = gt / se;
+    out[2] = gs / se;
+  }
+}
+
+cudaError_t launch_lg_begin(const gbns_batch &b, const gbns_lg_bufs &lg, long long total_chains, cudaStream_t s) {
+  if (total_chains <= 0) return cudaSuccess;
+  k_lg_init<<<(unsigned)((total_chains + 127) / 128), 128, 0, s>>>(b, lg, total_chains);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lg_steps(const gbns_batch &b, const gbns_lg_bufs &lg, long long total_chains, int pmax, int steps,
+                            cudaStream_t s) {
+  for (int q = 0; q < steps; ++q) {
+    k_lg_step<<<(unsigned)((total_chains + 127) / 128), 128, 0, s>>>(b, lg, total_chains);
+    if (lg.num_items > 0) {
+      if (pmax <= 32) k_lg_resid<32><<<lg.num_items, 256, 0, s>>>(b, lg);
+      else k_lg_resid<64><<<lg.num_items, 256, 0, s>>>(b, lg);
+    }
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const float *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
+                           int N, double log_tau, double log_sigma, double *out, double *ss, double *ry,
+                           cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(ss, 0, sizeof(double) * M, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ry, 0, sizeof(double) * M, s);
+  if (e != cudaSuccess) return e;
+  if (M > 0) {
+    dim3 grid((unsigned)((M + 63) / 64), (unsigned)((N + 63) / 64));
+    const float tau = (float)exp(log_tau);
+    if (P <= 32) k_adj_resid<32><<<grid, 256, 0, s>>>(U, M, P, Phi, y, N, tau, ss, ry);
+    else k_adj_resid<64><<<grid, 256, 0, s>>>(U, M, P, Phi, y, N, tau, ss, ry);
+  }
+  k_adj_reduce<<<1, 1024, 0, s>>>(log_w, M, N, log_sigma, ss, ry, out);
+  return cudaGetLastError();
+}
+
+}  // namespace gbns
+
+namespace {
+int lg_fail(int code, const char *msg) {
+  gbns::record_error(msg);
+  return code;
+}
+int lg_check(const gbns_batch *batch, const gbns_lg_bufs *lg) {
+  if (!batch || !lg || batch->num_runs <= 0 || lg->total_chains < 0 || lg->pmax < 1 || lg->pmax > 64 || !lg->flags ||
+      !lg->ss || !lg->W || !lg->u0 || !lg->dir || !lg->chains_left)
+    return lg_fail(-1, "gbns_lg: bad arguments (1 <= pmax <= 64, chain buffers required)");
+  return 0;
+}
+}  // namespace
+
+extern "C" {
+
+int gbns_lg_shell_begin(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
+  int rc = lg_check(batch, lg);
+  if (rc) return rc;
+  cudaError_t e = gbns::launch_lg_begin(*batch, *lg, lg->total_chains, (cudaStream_t)stream);
+  if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+// num_steps x (chain step + residual contraction); no host synchronisation.
+int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps, void *stream) {
+  int rc = lg_check(batch, lg);
+  if (rc) return rc;
+  if (num_steps < 0) return lg_fail(-1, "gbns_lg_steps: negative step count");
+  cudaError_t e = gbns::launch_lg_steps(*batch, *lg, lg->total_chains, lg->pmax, num_steps, (cudaStream_t)stream);
+  if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+int gbns_evidence_adjoint(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+                          const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
+                          double *ss_scratch_dev, double *ry_scratch_dev, void *stream) {
+  if (M < 0 || P < 1 || P > 64 || N < 1 || !out_dev || (M > 0 && (!U_dev || !log_w_dev || !ss_scratch_dev ||
+                                                                    !ry_scratch_dev)) || !Phi_dev || !y_dev)
+    return lg_fail(-1, "gbns_evidence_adjoint: bad arguments (1 <= P <= 64)");
+  cudaError_t e = gbns::launch_adjoint(U_dev, log_w_dev, M, P, Phi_dev, y_dev, N, log_tau, log_sigma, out_dev,
+                                       ss_scratch_dev, ry_scratch_dev, (cudaStream_t)stream);
+  if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+}  // extern "C"

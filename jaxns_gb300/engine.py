@@ -131,10 +131,11 @@ class NSBatch:
         caps = np.array([s.max_samples for s in specs], np.int64)
         if ns.max() > 4096:
             raise ValueError("at most 4096 live points per run")
+        fams = {s.family for s in specs}
+        self.lg = FAMILY_LINGAUSS in fams
+        if self.lg and len(fams) > 1:
+            raise ValueError("a batch holds either linear-Gaussian runs only or none")
         for s in specs:
-            if s.family not in (FAMILY_MVN, FAMILY_SHELLS):
-                raise ValueError("the slice engine runs the MVN and shells families; the linear-Gaussian "
-                                 "family uses the tensor-core path")
             _dbucket(s.D)
         live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])
         store_off = np.concatenate([[0], np.cumsum(caps)[:-1]])
@@ -212,6 +213,8 @@ class NSBatch:
         CH = int(chains_per_item)
         items = []
         for r, s in enumerate(specs):
+            if s.family == FAMILY_LINGAUSS:
+                continue
             b = s.family * 4 + _dbucket(s.D)
             # warp-cooperative buckets (MVN, D > 16): one chain per lane of the CTA (256 lanes
             # for D > 32, 512 for 16 < D <= 32), so the lanes of a CTA finish together
@@ -223,7 +226,7 @@ class NSBatch:
                 items.append((b, -s.D, r, c0, min(ch, s.shell_size - c0)))
         items.sort()
         arr = np.array([[it[2], it[3], it[4], 0] for it in items], np.int32).reshape(-1, 4)
-        self.items = torch.from_numpy(arr).to(dev)
+        self.items = torch.from_numpy(arr if len(arr) else np.zeros((1, 4), np.int32)).to(dev)
         bb = np.full(8, 0, np.int32)
         be = np.full(8, 0, np.int32)
         bk = np.array([it[0] for it in items])
@@ -250,6 +253,7 @@ class NSBatch:
         b.chains_per_item = CH
         b.max_evals_per_slice = int(max_evals_per_slice)
         self._b = b
+        self._lgb = self._alloc_lg(specs, ss, Ds, shell_off) if self.lg else None
         self._graphs: Dict[tuple, tuple] = {}
         self.timing = False
         self.shell_ms = 0.0
@@ -257,6 +261,35 @@ class NSBatch:
         self.iterations_run = 0
         self.kernel_launches = 0
         self._kernels_per_iter = 1 + int(np.count_nonzero(be > bb))
+
+    def _alloc_lg(self, specs, ss, Ds, shell_off):
+        """Lock-step chain state of the linear-Gaussian family + residual work items
+        (64 chains x 64 data rows per item)."""
+        dev = self.device
+        nc = int(ss.sum())
+        nd = int((ss * Ds).sum())
+        z = lambda n, dt=torch.float32: torch.zeros(max(n, 1), dtype=dt, device=dev)
+        self.lg_t = dict(j=z(nc, torch.int32), in_slice=z(nc, torch.int32), total=z(nc, torch.int32),
+                         flags=z(nc, torch.int32), left=z(nc), right=z(nc), t=z(nc), alpha=z(nc), logL0=z(nc),
+                         ck=z(2 * nc, torch.int32), after_key=z(2 * nc, torch.int32),
+                         slices_key=z(2 * nc, torch.int32), dir_key=z(2 * nc, torch.int32), u0=z(nd), dir=z(nd),
+                         W=z(nd), ss=z(nc, torch.float64), chains_left=z(len(specs), torch.int32))
+        items = []
+        for r, s in enumerate(specs):
+            for c0 in range(0, s.shell_size, 64):
+                for row0 in range(0, s.N, 64):
+                    items.append((r, c0, min(64, s.shell_size - c0), row0))
+        self.lg_items = torch.tensor(np.array(items, np.int32).reshape(-1, 4), device=dev)
+        g = _ffi.LGBufs()
+        for k, v in self.lg_t.items():
+            setattr(g, k, v.data_ptr())
+        g.items, g.num_items = self.lg_items.data_ptr(), len(items)
+        g.pmax = int(max(s.D for s in specs))
+        g.total_chains = nc
+        if g.pmax > 64:
+            raise ValueError("the linear-Gaussian path supports P <= 64")
+        self.lg_steps_run = 0
+        return g
 
     # ----------------------------------------------------------------- driving
     @staticmethod
@@ -268,9 +301,54 @@ class NSBatch:
         self.kernel_launches += 2
 
     def iterate(self, k: int):
+        if self.lg:
+            for _ in range(k):
+                self._lg_iteration(use_graph=False)
+            return
         _ffi.call("gbns_batch_iterate", ctypes.byref(self._b), int(k), self._stream())
         self.iterations_run += k
         self.kernel_launches += k * self._kernels_per_iter
+
+    def _lg_graph(self, k: int):
+        ent = self._graphs.get(("lg", k))
+        if ent is None:
+            g = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream())
+            with torch.cuda.graph(g, stream=side):
+                _ffi.call("gbns_lg_steps", ctypes.byref(self._b), ctypes.byref(self._lgb), int(k), self._stream())
+            torch.cuda.current_stream().wait_stream(side)
+            ent = (g, [])
+            self._graphs[("lg", k)] = ent
+        return ent[0]
+
+    def _lg_iteration(self, use_graph: bool = True, block: int = 64):
+        """One NS iteration of the linear-Gaussian batch: start the shell, advance every chain
+        in blocks of `block` likelihood evaluations until all chains are done, then merge."""
+        st = self.state()
+        active = (st["done"] == 0) & (st["phase"] == 1)
+        if not np.any(active):
+            return
+        _ffi.call("gbns_lg_shell_begin", ctypes.byref(self._b), ctypes.byref(self._lgb), self._stream())
+        self.kernel_launches += 1
+        cap = int(max(s.num_slices for s in self.specs)) * 2000
+        steps = 0
+        while True:
+            if use_graph:
+                self._lg_graph(block).replay()
+            else:
+                _ffi.call("gbns_lg_steps", ctypes.byref(self._b), ctypes.byref(self._lgb), int(block), self._stream())
+            steps += block
+            self.kernel_launches += 2 * block
+            left = self.lg_t["chains_left"].cpu().numpy()
+            if not np.any(left[active] > 0):
+                break
+            if steps > cap:
+                raise _ffi.GBNSError("linear-Gaussian shell did not finish within its step budget")
+        self.lg_steps_run += steps
+        _ffi.call("gbns_batch_merge", ctypes.byref(self._b), self._stream())
+        self.kernel_launches += 1
+        self.iterations_run += 1
 
     def _graph(self, k: int):
         """CUDA graph of k iterations; when timing, each iteration is captured as
@@ -347,6 +425,10 @@ class NSBatch:
             self._collect_timing()
             if done:
                 break
+            if self.lg:
+                self._lg_iteration(use_graph=use_graph)
+                done_it += 1
+                continue
             k = min(block, max_iterations - done_it)
             if use_graph:
                 self.iterate_graph(k)
