@@ -24,9 +24,13 @@
  *   gbns_random_bits64 / gbns_uniform / gbns_normal <- jax.random.bits/uniform/normal (test hooks)
  *   gbns_count_crossed_edges <- count_crossed_edges       internals/tree_structure.py:33-108
  *   gbns_evidence_stats   <- compute_evidence_stats       internals/shrinkage_statistics.py:131-157
- *   gbns_phiw_loglik      <- Model.forward of a linear-Gaussian model, batched over proposals
- *                            (the user likelihood N(y; Phi w, sigma^2 I); no reference kernel)
- *   gbns_evidence_adjoint <- jax.grad of EvidenceMaximisation's reweighted log-evidence
+ *   gbns_lg_shell_begin / gbns_lg_steps / gbns_lg_prepare_tc
+ *                         <- _collect_shell + UniDimSliceSampler for a linear-Gaussian model
+ *                            (the user likelihood N(y; Phi w, sigma^2 I), which a jaxns user
+ *                            writes in JAX; no reference kernel), chains in lock step with the
+ *                            Phi w contraction batched over all pending proposals
+ *   gbns_evidence_adjoint / gbns_evidence_adjoint_tc
+ *                         <- jax.grad of EvidenceMaximisation's reweighted log-evidence
  *                            experimental/evidence_maximisation.py:151-160 (weights :213)
  */
 #ifndef GBNS_H
@@ -57,7 +61,8 @@ enum gbns_status {
     GBNS_ERR_INIT_BUDGET = 1,    /* init rejection sampling ran out of its evaluation budget */
     GBNS_ERR_SHRINK_BUDGET = 2,  /* a slice shrink loop ran out of its evaluation budget      */
     GBNS_ERR_STORE_FULL = 4,     /* iteration budget / store capacity exhausted               */
-    GBNS_ERR_BAD_PARAM = 8
+    GBNS_ERR_BAD_PARAM = 8,
+    GBNS_ERR_WAIT_TIMEOUT = 16   /* a tensor-core kernel gave up waiting on its copies / MMAs  */
 };
 
 /* TerminationCondition (nested_samplers/common/types.py:26-60); has_* flags mark the
@@ -181,6 +186,17 @@ typedef struct {
     int num_items;
     int pmax;                               /* largest D (= P) over the runs, <= 64 */
     long long total_chains;                 /* sum of s over the runs */
+    /* Tensor-core (tcgen05) residual path, used when use_tc != 0 (after gbns_lg_prepare_tc
+     * has filled Phi_hi / Phi_lo).  Proposals and Phi are held as TF32 hi + lo parts, rows
+     * padded to 64 floats (256 B, zero beyond P); the contraction is hi*hi + hi*lo + lo*hi. */
+    int use_tc;
+    int num_items_tc;
+    const int *items_tc;                    /* [num_items_tc * 4]: (run, first chain, count <= 128, first row);
+                                               first chain a multiple of 128, first row a multiple of 256 */
+    float *W_hi, *W_lo;                     /* [total_chains * 64], row = global chain index */
+    float *Phi_hi, *Phi_lo;                 /* [total_rows * 64] */
+    const long long *row_base;              /* [R] first row of each run in Phi_hi / Phi_lo */
+    long long total_rows;                   /* sum of N over the runs */
 } gbns_lg_bufs;
 
 /* results buffers (device) */
@@ -257,6 +273,9 @@ int gbns_count_crossed_edges_static(const int *sender_dev, const float *log_L_de
  *      uni_slice_sampler.py:343-441) for a likelihood evaluated in batches */
 int gbns_lg_shell_begin(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps, void *stream);
+/* Split each run's Phi (fparams) into the TF32 hi/lo row-padded copies lg->Phi_hi / Phi_lo
+ * used by the tensor-core residual path.  Call once per batch, before the first step. */
+int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 
 /* Reweighted fixed-dead-point evidence of the linear-Gaussian model and its gradient
  * (experimental/evidence_maximisation.py:151-160, weights :213):
@@ -266,6 +285,14 @@ int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps
 int gbns_evidence_adjoint(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
                           const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
                           double *ss_scratch_dev, double *ry_scratch_dev, void *stream);
+/* The same on the tcgen05 tensor cores (3xTF32 contraction).  Extra scratch, with
+ * ld = 32 for P <= 32 and 64 otherwise: w_scratch [2 * M * ld] floats, phi_scratch
+ * [2 * N * ld] floats; status_dev: one int, GBNS_ERR_WAIT_TIMEOUT is or-ed in if a wait of
+ * the kernel timed out (the outputs are then invalid).  M < 2^31. */
+int gbns_evidence_adjoint_tc(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+                             const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
+                             double *ss_scratch_dev, double *ry_scratch_dev, float *w_scratch_dev,
+                             float *phi_scratch_dev, int *status_dev, void *stream);
 int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,
                         int nmax, gbns_evcalc *final_dev, double *log_X_mean_dev, double *log_dZ_mean_dev,
                         double *log_Z_mean_dev, void *stream);

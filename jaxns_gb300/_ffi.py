@@ -68,7 +68,10 @@ class LGBufs(ctypes.Structure):
                 ("left", c_void_p), ("right", c_void_p), ("t", c_void_p), ("alpha", c_void_p), ("logL0", c_void_p),
                 ("ck", c_void_p), ("after_key", c_void_p), ("slices_key", c_void_p), ("dir_key", c_void_p),
                 ("u0", c_void_p), ("dir", c_void_p), ("W", c_void_p), ("ss", c_void_p), ("chains_left", c_void_p),
-                ("items", c_void_p), ("num_items", c_int), ("pmax", c_int), ("total_chains", c_ll)]
+                ("items", c_void_p), ("num_items", c_int), ("pmax", c_int), ("total_chains", c_ll),
+                ("use_tc", c_int), ("num_items_tc", c_int), ("items_tc", c_void_p), ("W_hi", c_void_p),
+                ("W_lo", c_void_p), ("Phi_hi", c_void_p), ("Phi_lo", c_void_p), ("row_base", c_void_p),
+                ("total_rows", c_ll)]
 
 
 class ResultsBufs(ctypes.Structure):
@@ -81,7 +84,8 @@ EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2
             "gbns_uniform", "gbns_normal", "gbns_forward", "gbns_batch_init", "gbns_batch_iterate",
             "gbns_batch_finalize", "gbns_batch_results", "gbns_slice_shell", "gbns_count_crossed_edges",
             "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
-            "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint")
+            "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint",
+            "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc")
 
 _lib = None
 

@@ -36,8 +36,12 @@ class DeadSet:
                        y=torch.as_tensor(np.asarray(y, np.float32), device=dev).contiguous())
 
 
-def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float):
-    """(log Z(theta), d log Z / d log tau, d log Z / d log sigma) on the device, FP64."""
+def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float, tensor_cores: bool = True,
+                      check: bool = True):
+    """(log Z(theta), d log Z / d log tau, d log Z / d log sigma) on the device, FP64.
+    tensor_cores: the per-point residuals |y - Phi w|^2 as a 3xTF32 tcgen05 GEMM
+    (gbns_evidence_adjoint_tc) instead of fp32 CUDA-core tiles (gbns_evidence_adjoint).
+    check: synchronise and raise if a tensor-core wait timed out."""
     M, P = ds.U.shape
     N = ds.Phi.shape[0]
     dev = ds.U.device
@@ -45,9 +49,19 @@ def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float):
     ss = torch.empty(max(M, 1), dtype=torch.float64, device=dev)
     ry = torch.empty(max(M, 1), dtype=torch.float64, device=dev)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
-    _ffi.call("gbns_evidence_adjoint", p(ds.U), p(ds.log_w), ctypes.c_longlong(M), ctypes.c_int(P), p(ds.Phi),
-              p(ds.y), ctypes.c_int(N), ctypes.c_double(float(log_tau)), ctypes.c_double(float(log_sigma)), p(out),
-              p(ss), p(ry), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = [p(ds.U), p(ds.log_w), ctypes.c_longlong(M), ctypes.c_int(P), p(ds.Phi), p(ds.y), ctypes.c_int(N),
+            ctypes.c_double(float(log_tau)), ctypes.c_double(float(log_sigma)), p(out), p(ss), p(ry)]
+    if not tensor_cores:
+        _ffi.call("gbns_evidence_adjoint", *args, stream)
+        return out
+    ld = 32 if P <= 32 else 64
+    ws = torch.empty(max(2 * M * ld, 1), dtype=torch.float32, device=dev)
+    ps = torch.empty(2 * N * ld, dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    _ffi.call("gbns_evidence_adjoint_tc", *args, p(ws), p(ps), p(status), stream)
+    if check and int(status.item()) != 0:
+        raise _ffi.GBNSError(f"gbns_evidence_adjoint_tc: device status {int(status.item())} (wait timed out)")
     return out
 
 

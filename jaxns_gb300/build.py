@@ -12,7 +12,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(_HERE, "csrc")
 OUT_DIR = os.path.join(_HERE, "_lib")
 OBJ_DIR = os.path.join(os.path.dirname(_HERE), "_build", "obj")
-SOURCES = ["gbns_slice.cu", "gbns_slice_warp.cu", "gbns_ns.cu", "gbns_results.cu", "gbns_phiw.cu", "gbns_api.cu",
+SOURCES = ["gbns_slice.cu", "gbns_slice_warp.cu", "gbns_ns.cu", "gbns_results.cu", "gbns_phiw.cu", "gbns_phiw_tc.cu", "gbns_api.cu",
            "gbns_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]

@@ -426,6 +426,16 @@ __device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ 
 //  MVN:     [mu(D), Linv(D*D row-major, lower), c0]   c0 = -sum log L_ii - D/2 log 2pi
 //  SHELLS:  [c1(D), c2(D), R, w, norm]                 norm = log sqrt(2 pi w^2)
 //  LINGAUSS:[Phi(N*D row-major), y(N), sigma]
+// x = hi + lo with hi and lo both TF32 (round to nearest, ties away): the operand split of
+// the 3xTF32 tensor-core contraction (hi*hi + hi*lo + lo*hi).
+__device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
+  uint32_t h, l;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(h) : "f"(x));
+  hi = __uint_as_float(h);
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(l) : "f"(x - hi));
+  lo = __uint_as_float(l);
+}
+
 __device__ __forceinline__ float prior_quantile(int kind, float a, float b, float u) {
   if (kind == GBNS_PRIOR_UNIFORM) return fmaf(b, u, a);
   return fmaf(b, GBNS_SQRT2F * erfinvf(fmaf(2.0f, u, -1.0f)), a);

@@ -16,6 +16,14 @@ cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long l
                                        int *num_live, long long *scratch_ll, int *scratch_i, cudaStream_t stream);
 cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream);
+cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
+cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t stream);
+cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
+cudaError_t launch_adjoint_reduce(const double *log_w, long long M, int N, double log_sigma, const double *ss,
+                                  const double *ry, double *out, cudaStream_t stream);
+cudaError_t launch_adjoint_tc(const float *U, const double *log_w, long long M, int P, const float *Phi,
+                              const float *y, int N, double log_tau, double log_sigma, double *out, double *ss,
+                              double *ry, float *w_scratch, float *phi_scratch, int *status, cudaStream_t stream);
 // Sets the thread-local message returned by gbns_last_error().
 void record_error(const char *msg);
 cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n,

@@ -191,7 +191,12 @@ __global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
     t = fmaf(uniform01(bits64(tk, 0u)), right - left, left);
     const int *kind = b.prior_kind + rd.prior_off;
     const float *pa = b.prior_a + rd.prior_off, *pb = b.prior_b + rd.prior_off;
-    for (int p = 0; p < P; ++p) W[p] = prior_quantile(kind[p], pa[p], pb[p], fmaf(t, d[p], u0[p]));
+    if (lg.use_tc) {
+      float *wh = lg.W_hi + (size_t)g * 64, *wl = lg.W_lo + (size_t)g * 64;
+      for (int p = 0; p < P; ++p) tf32_split(prior_quantile(kind[p], pa[p], pb[p], fmaf(t, d[p], u0[p])), wh[p], wl[p]);
+    } else {
+      for (int p = 0; p < P; ++p) W[p] = prior_quantile(kind[p], pa[p], pb[p], fmaf(t, d[p], u0[p]));
+    }
     flags |= LG_PENDING;
   }
   lg.flags[g] = flags;
@@ -350,8 +355,15 @@ cudaError_t launch_lg_begin(const gbns_batch &b, const gbns_lg_bufs &lg, long lo
   return cudaGetLastError();
 }
 
+cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
+  if (lg.total_chains > 0)
+    k_lg_step<<<(unsigned)((lg.total_chains + 127) / 128), 128, 0, s>>>(b, lg, lg.total_chains);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_lg_steps(const gbns_batch &b, const gbns_lg_bufs &lg, long long total_chains, int pmax, int steps,
                             cudaStream_t s) {
+  if (lg.use_tc) return launch_lg_steps_tc(b, lg, steps, s);
   for (int q = 0; q < steps; ++q) {
     k_lg_step<<<(unsigned)((total_chains + 127) / 128), 128, 0, s>>>(b, lg, total_chains);
     if (lg.num_items > 0) {
@@ -374,6 +386,11 @@ cudaError_t launch_adjoint(const float *U, const double *log_w, long long M, int
     if (P <= 32) k_adj_resid<32><<<grid, 256, 0, s>>>(U, M, P, Phi, y, N, tau, ss, ry);
     else k_adj_resid<64><<<grid, 256, 0, s>>>(U, M, P, Phi, y, N, tau, ss, ry);
   }
+  return launch_adjoint_reduce(log_w, M, N, log_sigma, ss, ry, out, s);
+}
+
+cudaError_t launch_adjoint_reduce(const double *log_w, long long M, int N, double log_sigma, const double *ss,
+                                  const double *ry, double *out, cudaStream_t s) {
   k_adj_reduce<<<1, 1024, 0, s>>>(log_w, M, N, log_sigma, ss, ry, out);
   return cudaGetLastError();
 }
@@ -389,6 +406,9 @@ int lg_check(const gbns_batch *batch, const gbns_lg_bufs *lg) {
   if (!batch || !lg || batch->num_runs <= 0 || lg->total_chains < 0 || lg->pmax < 1 || lg->pmax > 64 || !lg->flags ||
       !lg->ss || !lg->W || !lg->u0 || !lg->dir || !lg->chains_left)
     return lg_fail(-1, "gbns_lg: bad arguments (1 <= pmax <= 64, chain buffers required)");
+  if (lg->use_tc && (!lg->W_hi || !lg->W_lo || !lg->Phi_hi || !lg->Phi_lo || !lg->row_base || lg->total_rows < 1 ||
+                     lg->num_items_tc < 0 || (lg->num_items_tc > 0 && !lg->items_tc)))
+    return lg_fail(-1, "gbns_lg: use_tc needs W_hi, W_lo, Phi_hi, Phi_lo, row_base and items_tc");
   return 0;
 }
 }  // namespace

@@ -1,0 +1,436 @@
+// gbns_phiw_tc.cu -- the Phi w residual contraction on the 5th-generation tensor cores.
+//
+// For a tile of 128 points (slice proposals, or dead points for the adjoint) and 256 data
+// rows, D[point][row] = w_point . Phi_row is one tcgen05 GEMM with K = P <= 64:
+//   * w and Phi are held as TF32 hi + lo parts (x = hi + lo, both rounded to TF32), rows
+//     padded with zeros to a multiple of 32 floats, so one K block is one 128-byte row;
+//   * one thread issues the TMA loads of the four K-major tiles (128B swizzle, one mbarrier
+//     with an expected byte count) and then, per K step of 8, the three products
+//     hi*hi + hi*lo + lo*hi as tcgen05.mma kind::tf32 into one FP32 accumulator of
+//     128 lanes x 256 columns in tensor memory (3xTF32: fp32-level accuracy);
+//   * the four warps read their 32 lanes back with tcgen05.ld (thread = point, 32 rows per
+//     load), form r = y - Phi w, and add sum r^2 and sum r y to the point's FP64 totals.
+// Every wait is bounded: on time-out the kernel sets GBNS_ERR_WAIT_TIMEOUT, skips the
+// epilogue, frees its tensor memory and returns.
+#include <cuda.h>
+#include <cstdio>
+#include <mutex>
+#include "gbns_device.cuh"
+#include "gbns_launch.h"
+
+namespace gbns {
+
+constexpr int TC_M = 128;                            // points per tile (tensor-memory lanes)
+constexpr int TC_N = 256;                            // data rows per tile (tensor-memory columns)
+constexpr int TC_KB = 32;                            // floats per 128-byte swizzled row (one K block)
+constexpr unsigned TC_A_BYTES = TC_M * TC_KB * 4;    // 16 KB
+constexpr unsigned TC_B_BYTES = TC_N * TC_KB * 4;    // 32 KB
+constexpr unsigned TC_KB_BYTES = 2 * TC_A_BYTES + 2 * TC_B_BYTES;  // hi + lo of both operands: 96 KB
+constexpr long long TC_WAIT_CYCLES = 2000000000ll;   // ~1 s at the maximum SM clock
+
+// Instruction descriptor of tcgen05.mma kind::tf32: D f32 (bits 4-5 = 1), A and B TF32
+// (bits 7-9, 10-12 = 2), both K-major (bits 15, 16 = 0), N >> 3 at bits 17-22, M >> 4 at
+// bits 24-28.
+constexpr uint32_t TC_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
+                              ((uint32_t)(TC_M >> 4) << 24);
+
+struct alignas(128) TcMaps {
+  CUtensorMap a_hi, a_lo, b_hi, b_lo;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor of a K-major tile in the 128-byte swizzle layout written
+// by TMA: start address >> 4 (bits 0-13), leading-byte offset 16 B (unused for this layout;
+// bits 16-29), stride between 8-row groups 1024 B (bits 32-45), descriptor version 1
+// (bit 46), swizzle mode 2 = 128 B (bits 61-63).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)(16 >> 4) << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         (1ull << 46) | (2ull << 61);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+
+// Waits for phase `parity` of the barrier to complete; false after TC_WAIT_CYCLES.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(TC_IDESC), "r"(accumulate)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 consecutive fp32 columns of this warp's 32 lanes: thread t gets lane (base lane + t).
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+      "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int j = 0; j < 32; ++j) v[j] = __uint_as_float(r[j]);
+}
+
+// One 128-point x 256-row tile.  a_row / b_row: first row of the tile in the point and Phi
+// tensor maps; nkb K blocks of 32 are loaded, nk8 K steps of 8 are multiplied; npts points
+// and nrows rows are valid.  Must be called by all 128 threads of the CTA.
+__device__ void tc_resid_tile(const TcMaps &maps, int a_row, int b_row, int nkb, int nk8, int npts, int nrows,
+                              const float *__restrict__ y, double *ss_out, double *ry_out, int *status) {
+  extern __shared__ unsigned char tc_dyn[];
+  __shared__ __align__(8) unsigned long long bars[2];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int fail;
+  __shared__ float ys[TC_N];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t tiles = (smem_u32(tc_dyn) + 1023u) & ~1023u;  // 1024-byte aligned for the 128B swizzle
+  const uint32_t bar_tma = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+
+  if (tid == 0) {
+    mbar_init(bar_tma, 1);
+    mbar_init(bar_mma, 1);
+    fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"((uint32_t)TC_N)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  for (int q = tid; q < TC_N; q += blockDim.x) ys[q] = (q < nrows) ? y[q] : 0.0f;
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+
+  if (tid == 0) {
+    // lane 0 of warp 0 issues the copies and the MMAs; lanes 1-31 wait for it at __syncwarp
+    mbar_expect_tx(bar_tma, (uint32_t)nkb * TC_KB_BYTES);
+    for (int kb = 0; kb < nkb; ++kb) {
+      const uint32_t base = tiles + (uint32_t)kb * TC_KB_BYTES;
+      tma_load_2d(base, &maps.a_hi, kb * TC_KB, a_row, bar_tma);
+      tma_load_2d(base + TC_A_BYTES, &maps.a_lo, kb * TC_KB, a_row, bar_tma);
+      tma_load_2d(base + 2 * TC_A_BYTES, &maps.b_hi, kb * TC_KB, b_row, bar_tma);
+      tma_load_2d(base + 2 * TC_A_BYTES + TC_B_BYTES, &maps.b_lo, kb * TC_KB, b_row, bar_tma);
+    }
+    if (mbar_wait(bar_tma, 0)) {
+      tc_fence_after();
+      uint32_t acc = 0;
+      for (int k8 = 0; k8 < nk8; ++k8) {
+        const int kb = k8 >> 2;
+        const uint32_t base = tiles + (uint32_t)kb * TC_KB_BYTES, off = (uint32_t)(k8 & 3) * 32u;
+        const uint64_t ah = smem_desc(base + off), al = smem_desc(base + TC_A_BYTES + off);
+        const uint64_t bh = smem_desc(base + 2 * TC_A_BYTES + off);
+        const uint64_t bl = smem_desc(base + 2 * TC_A_BYTES + TC_B_BYTES + off);
+        tc_mma(tmem, al, bh, acc);
+        tc_mma(tmem, ah, bl, 1u);
+        tc_mma(tmem, ah, bh, 1u);
+        acc = 1u;
+      }
+      tc_commit(bar_mma);
+    } else {
+      // the copies did not land: report, give them one more bounded wait, release the others
+      fail = 1;
+      atomicOr(status, (int)GBNS_ERR_WAIT_TIMEOUT);
+      mbar_wait(bar_tma, 0);
+      mbar_arrive(bar_mma);
+    }
+  }
+  __syncwarp();
+  bool ok = mbar_wait(bar_mma, 0);
+  ok = __all_sync(0xffffffffu, ok && fail == 0);
+  tc_fence_after();
+  if (ok) {
+    const int pt = warp * 32 + lane;
+    const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16);
+    const int nch = (nrows + 31) >> 5;
+    double s1 = 0.0, s2 = 0.0;
+    for (int ch = 0; ch < nch; ++ch) {
+      float v[32];
+      tc_ld32(taddr + (uint32_t)(ch * 32), v);
+      float p1 = 0.0f, p2 = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) {
+        const int row = ch * 32 + j;
+        if (row < nrows) {
+          const float yy = ys[row];
+          const float rr = yy - v[j];
+          p1 = fmaf(rr, rr, p1);
+          p2 = fmaf(rr, yy, p2);
+        }
+      }
+      s1 += (double)p1;
+      s2 += (double)p2;
+    }
+    if (pt < npts) {
+      atomicAdd(&ss_out[pt], s1);
+      if (ry_out) atomicAdd(&ry_out[pt], s2);
+    }
+  } else if (tid == 32) {
+    atomicOr(status, (int)GBNS_ERR_WAIT_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)TC_N) : "memory");
+  }
+}
+
+// Sampler step: the pending proposals of each (run, 128-chain tile, 256-row tile) item.
+__global__ void __launch_bounds__(128) k_lg_resid_tc(const __grid_constant__ TcMaps maps, gbns_batch b,
+                                                     gbns_lg_bufs lg) {
+  const int *it = lg.items_tc + 4 * (size_t)blockIdx.x;
+  const int r = it[0], c0 = it[1], nc = it[2], row0 = it[3];
+  const gbns_run_desc &rd = b.runs[r];
+  gbns_run_state &st = b.state[r];
+  if (st.done || st.phase != 1) return;
+  const int P = rd.D, N = rd.N;
+  const float *y = b.fparams + rd.param_off + (size_t)N * P;
+  tc_resid_tile(maps, (int)(rd.shell_off + c0), (int)(lg.row_base[r] + row0), (P + TC_KB - 1) / TC_KB, (P + 7) / 8,
+                nc, min(TC_N, N - row0), y + row0, lg.ss + rd.shell_off + c0, nullptr, &st.status);
+}
+
+// Adjoint: all dead points (blockIdx.x: 128-point tile) against all rows (blockIdx.y).
+__global__ void __launch_bounds__(128) k_adj_resid_tc(const __grid_constant__ TcMaps maps, long long M, int P, int N,
+                                                      const float *y, double *ss, double *ry, int *status) {
+  const long long p0 = (long long)blockIdx.x * TC_M;
+  const int row0 = blockIdx.y * TC_N;
+  tc_resid_tile(maps, (int)p0, row0, (P + TC_KB - 1) / TC_KB, (P + 7) / 8, (int)min((long long)TC_M, M - p0),
+                min(TC_N, N - row0), y + row0, ss + p0, ry + p0, status);
+}
+
+// Phi of every run -> TF32 hi/lo rows of 64 floats (zero beyond P).
+__global__ void k_split_phi(gbns_batch b, gbns_lg_bufs lg) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= lg.total_rows * 64) return;
+  const long long grow = q >> 6;
+  const int k = (int)(q & 63);
+  int lo = 0, hi = b.num_runs;
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (lg.row_base[mid] <= grow) lo = mid; else hi = mid;
+  }
+  const gbns_run_desc &rd = b.runs[lo];
+  const long long row = grow - lg.row_base[lo];
+  float h = 0.0f, l = 0.0f;
+  if (row < rd.N && k < rd.D) tf32_split(b.fparams[rd.param_off + row * rd.D + k], h, l);
+  lg.Phi_hi[q] = h;
+  lg.Phi_lo[q] = l;
+}
+
+// Dead points for the adjoint: w = tau * sqrt(2) * erfinv(2u - 1) (the Normal(0, tau^2)
+// quantile), and Phi, both as TF32 hi/lo rows of ld floats.
+__global__ void k_adj_split(const float *U, long long M, int P, const float *Phi, int N, float tau, int ld,
+                            float *w_hi, float *w_lo, float *phi_hi, float *phi_lo) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long nw = M * ld, np = (long long)N * ld;
+  if (q >= nw + np) return;
+  float h = 0.0f, l = 0.0f;
+  if (q < nw) {
+    const long long i = q / ld;
+    const int k = (int)(q % ld);
+    if (k < P) tf32_split(tau * (GBNS_SQRT2F * erfinvf(fmaf(2.0f, U[i * P + k], -1.0f))), h, l);
+    w_hi[q] = h;
+    w_lo[q] = l;
+  } else {
+    const long long e = q - nw, row = e / ld;
+    const int k = (int)(e % ld);
+    if (k < P) tf32_split(Phi[row * P + k], h, l);
+    phi_hi[e] = h;
+    phi_lo[e] = l;
+  }
+}
+
+// ----------------------------------------------------------------------------- host side
+
+namespace {
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
+// rows x ld fp32 matrix (row stride ld * 4 bytes), boxes of 32 floats x box_rows rows,
+// 128-byte swizzle, zero fill outside.
+bool encode_rows(CUtensorMap *m, const float *base, long long rows, int ld, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn || !base || rows < 1 || (ld != 32 && ld != 64) || ((uintptr_t)base & 15)) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)ld, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 4};
+  const cuuint32_t box[2] = {(cuuint32_t)TC_KB, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void *)base, dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// The dynamic shared-memory limit of the two tile kernels, raised once per device.
+cudaError_t set_smem_attrs() {
+  static std::mutex mu;
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaError_t err = cudaGetDevice(&dev);
+  if (err != cudaSuccess) return err;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(mu);
+  if (done[dev]) return cudaSuccess;
+  const int bytes = 2 * (int)TC_KB_BYTES + 1024;
+  err = cudaFuncSetAttribute(k_lg_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (err == cudaSuccess) err = cudaFuncSetAttribute(k_adj_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (err == cudaSuccess) done[dev] = true;
+  return err;
+}
+
+}  // namespace
+
+cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
+  cudaError_t e = set_smem_attrs();
+  if (e != cudaSuccess) return e;
+  const long long n = lg.total_rows * 64;
+  if (n > 0) k_split_phi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, lg);
+  return cudaGetLastError();
+}
+
+// steps x (chain step + tensor-core residual over lg.items_tc); the TMA descriptors are
+// encoded once per call from lg's buffers.
+cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t s) {
+  cudaError_t e = set_smem_attrs();
+  if (e != cudaSuccess) return e;
+  TcMaps maps;
+  if (!encode_rows(&maps.a_hi, lg.W_hi, lg.total_chains, 64, TC_M) ||
+      !encode_rows(&maps.a_lo, lg.W_lo, lg.total_chains, 64, TC_M) ||
+      !encode_rows(&maps.b_hi, lg.Phi_hi, lg.total_rows, 64, TC_N) ||
+      !encode_rows(&maps.b_lo, lg.Phi_lo, lg.total_rows, 64, TC_N))
+    return cudaErrorInvalidValue;
+  const int nkb = lg.pmax > TC_KB ? 2 : 1;
+  for (int q = 0; q < steps; ++q) {
+    e = launch_lg_step_kernel(b, lg, s);
+    if (e != cudaSuccess) return e;
+    if (lg.num_items_tc > 0) k_lg_resid_tc<<<lg.num_items_tc, 128, nkb * TC_KB_BYTES + 1024, s>>>(maps, b, lg);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_tc(const float *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
+                              int N, double log_tau, double log_sigma, double *out, double *ss, double *ry,
+                              float *w_scratch, float *phi_scratch, int *status, cudaStream_t s) {
+  cudaError_t e = set_smem_attrs();
+  if (e == cudaSuccess) e = cudaMemsetAsync(ss, 0, sizeof(double) * M, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(ry, 0, sizeof(double) * M, s);
+  if (e != cudaSuccess) return e;
+  const int ld = P > TC_KB ? 64 : 32;
+  if (M > 0) {
+    float *w_hi = w_scratch, *w_lo = w_scratch + M * ld;
+    float *p_hi = phi_scratch, *p_lo = phi_scratch + (long long)N * ld;
+    const long long tot = (M + N) * (long long)ld;
+    k_adj_split<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(U, M, P, Phi, N, (float)exp(log_tau), ld, w_hi, w_lo,
+                                                              p_hi, p_lo);
+    TcMaps maps;
+    if (!encode_rows(&maps.a_hi, w_hi, M, ld, TC_M) || !encode_rows(&maps.a_lo, w_lo, M, ld, TC_M) ||
+        !encode_rows(&maps.b_hi, p_hi, N, ld, TC_N) || !encode_rows(&maps.b_lo, p_lo, N, ld, TC_N))
+      return cudaErrorInvalidValue;
+    dim3 grid((unsigned)((M + TC_M - 1) / TC_M), (unsigned)((N + TC_N - 1) / TC_N));
+    k_adj_resid_tc<<<grid, 128, (ld / TC_KB) * TC_KB_BYTES + 1024, s>>>(maps, M, P, N, y, ss, ry, status);
+  }
+  return launch_adjoint_reduce(log_w, M, N, log_sigma, ss, ry, out, s);
+}
+
+}  // namespace gbns
+
+namespace {
+int tc_fail(int code, const char *msg) {
+  gbns::record_error(msg);
+  return code;
+}
+}  // namespace
+
+extern "C" {
+
+int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
+  if (!batch || !lg || batch->num_runs <= 0 || !lg->Phi_hi || !lg->Phi_lo || !lg->row_base || lg->total_rows < 1)
+    return tc_fail(-1, "gbns_lg_prepare_tc: bad arguments (Phi_hi, Phi_lo, row_base and total_rows >= 1 required)");
+  cudaError_t e = gbns::lg_tc_prepare(*batch, *lg, (cudaStream_t)stream);
+  if (e != cudaSuccess) return tc_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+int gbns_evidence_adjoint_tc(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+                             const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
+                             double *ss_scratch_dev, double *ry_scratch_dev, float *w_scratch_dev,
+                             float *phi_scratch_dev, int *status_dev, void *stream) {
+  if (M < 0 || M > 2147483647ll || P < 1 || P > 64 || N < 1 || !out_dev || !Phi_dev || !y_dev || !status_dev ||
+      !phi_scratch_dev ||
+      (M > 0 && (!U_dev || !log_w_dev || !ss_scratch_dev || !ry_scratch_dev || !w_scratch_dev)))
+    return tc_fail(-1, "gbns_evidence_adjoint_tc: bad arguments (1 <= P <= 64, 0 <= M < 2^31, scratch required)");
+  cudaError_t e = gbns::launch_adjoint_tc(U_dev, log_w_dev, M, P, Phi_dev, y_dev, N, log_tau, log_sigma, out_dev,
+                                          ss_scratch_dev, ry_scratch_dev, w_scratch_dev, phi_scratch_dev, status_dev,
+                                          (cudaStream_t)stream);
+  if (e != cudaSuccess) return tc_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+}  // extern "C"

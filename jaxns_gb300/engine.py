@@ -30,7 +30,8 @@ PRIOR_UNIFORM = 0
 PRIOR_NORMAL = 1
 
 STATUS_BITS = {1: "init rejection budget exhausted", 2: "slice shrink budget exhausted",
-               4: "store full", 8: "bad parameter (uniform phase would need iterations)"}
+               4: "store full", 8: "bad parameter (uniform phase would need iterations)",
+               16: "tensor-core kernel wait timed out"}
 
 _TC_NAMES = ("ess", "evidence_uncert", "dlogZ", "max_samples", "max_num_likelihood_evaluations",
              "log_L_contour", "efficiency_threshold", "rtol", "atol", "peak_XL_frac")
@@ -116,7 +117,7 @@ class NSBatch:
     """Device state of R independent runs."""
 
     def __init__(self, specs: List[RunSpec], device="cuda", chains_per_item: int = 64,
-                 max_evals_per_slice: int = 100000, wide_chains_per_item: int = 0):
+                 max_evals_per_slice: int = 100000, wide_chains_per_item: int = 0, lg_tensor_cores: bool = True):
         if not specs:
             raise ValueError("no runs")
         self.specs = specs
@@ -253,7 +254,7 @@ class NSBatch:
         b.chains_per_item = CH
         b.max_evals_per_slice = int(max_evals_per_slice)
         self._b = b
-        self._lgb = self._alloc_lg(specs, ss, Ds, shell_off) if self.lg else None
+        self._lgb = self._alloc_lg(specs, ss, Ds, shell_off, lg_tensor_cores) if self.lg else None
         self._graphs: Dict[tuple, tuple] = {}
         self.timing = False
         self.shell_ms = 0.0
@@ -262,9 +263,10 @@ class NSBatch:
         self.kernel_launches = 0
         self._kernels_per_iter = 1 + int(np.count_nonzero(be > bb))
 
-    def _alloc_lg(self, specs, ss, Ds, shell_off):
-        """Lock-step chain state of the linear-Gaussian family + residual work items
-        (64 chains x 64 data rows per item)."""
+    def _alloc_lg(self, specs, ss, Ds, shell_off, tensor_cores=True):
+        """Lock-step chain state of the linear-Gaussian family + residual work items:
+        tensor cores (tcgen05, 128 chains x 256 data rows per item, proposals and Phi as
+        TF32 hi/lo rows of 64 floats) or fp32 CUDA cores (64 chains x 64 rows per item)."""
         dev = self.device
         nc = int(ss.sum())
         nd = int((ss * Ds).sum())
@@ -288,6 +290,25 @@ class NSBatch:
         g.total_chains = nc
         if g.pmax > 64:
             raise ValueError("the linear-Gaussian path supports P <= 64")
+        self.lg_tc = bool(tensor_cores)
+        if self.lg_tc:
+            Ns = np.array([s.N for s in specs], np.int64)
+            row_base = np.concatenate([[0], np.cumsum(Ns)[:-1]]).astype(np.int64)
+            rows = int(Ns.sum())
+            items_tc = []
+            for r, s in enumerate(specs):
+                for c0 in range(0, s.shell_size, 128):
+                    for row0 in range(0, s.N, 256):
+                        items_tc.append((r, c0, min(128, s.shell_size - c0), row0))
+            self.lg_tc_t = dict(W_hi=z(nc * 64), W_lo=z(nc * 64), Phi_hi=z(rows * 64), Phi_lo=z(rows * 64),
+                                row_base=torch.tensor(row_base, device=dev),
+                                items_tc=torch.tensor(np.array(items_tc, np.int32).reshape(-1, 4), device=dev))
+            for k, v in self.lg_tc_t.items():
+                setattr(g, k, v.data_ptr())
+            g.num_items_tc = len(items_tc)
+            g.total_rows = rows
+            g.use_tc = 1
+            _ffi.call("gbns_lg_prepare_tc", ctypes.byref(self._b), ctypes.byref(g), self._stream())
         self.lg_steps_run = 0
         return g
 

@@ -113,11 +113,39 @@ def test_adjoint_against_oracle_and_fd(gpu_lib, oracle_mod):
     np.testing.assert_allclose(theta.grad.numpy(), out[1:], rtol=1e-12)
 
 
+def _gradient_standard_error(ds, log_tau, log_sigma):
+    """Standard error of the reweighted gradient estimate sum_i p_i g_i of one run: the
+    weighted spread of the per-point gradients g_i = d log L(U_i) / d theta over the Kish
+    effective sample size of p (FP64 on the device; test-side only)."""
+    M, P = ds.U.shape
+    N = ds.Phi.shape[0]
+    tau, s2 = np.exp(log_tau), np.exp(2 * log_sigma)
+    Phi, y = ds.Phi.double(), ds.y.double()
+    ss, rp = [], []
+    for i0 in range(0, M, 8192):                    # [8192, N] FP64 blocks
+        w = tau * np.sqrt(2.0) * torch.erfinv(2.0 * ds.U[i0:i0 + 8192].double() - 1.0)
+        Pw = w @ Phi.T
+        r = y[None, :] - Pw
+        ss.append((r * r).sum(1))
+        rp.append((r * Pw).sum(1))
+    ss, rp = torch.cat(ss), torch.cat(rp)
+    g = torch.stack([rp / s2, ss / s2 - N], 1)
+    a = -0.5 * ss / s2 + ds.log_w
+    p = torch.softmax(a, 0)
+    mean = (p[:, None] * g).sum(0)
+    var = (p[:, None] * (g - mean) ** 2).sum(0)
+    ess = 1.0 / (p * p).sum()
+    return (torch.sqrt(var / ess)).cpu().numpy(), float(ess)
+
+
 def test_config4_blr_evidence_and_gradient(gpu_lib):
     """Config 4: Phi in R^{4096x32} ~ N(0,1), w_true ~ N(0, I), y = Phi w + eps (sigma = 0.5),
     prior w ~ N(0, tau^2 I), (log tau, log sigma) = (0, log 0.5), 1024 live points, default
-    termination (dlogZ < log(1 + 1e-3)): log Z against the analytic evidence; the reweighted-evidence gradient against
-    the analytic gradient (relative error reported with the run's own noise floor)."""
+    termination (dlogZ < log(1 + 1e-3)): log Z against the analytic evidence; the
+    reweighted-evidence gradient against the analytic gradient within the run's own Monte
+    Carlo error.  The per-point d log L / d log tau has a posterior spread of ~|Phi w| / sigma
+    (~700 here) around a mean of ~-5, so one run's tau gradient carries an error of order 10;
+    the sigma gradient is far less noisy."""
     import jaxns_gb300 as gb
     from jaxns_gb300.adjoint import DeadSet, blr_log_evidence, evidence_and_grad
     Phi, y = blr(4096, 32, seed=2024)
@@ -130,8 +158,98 @@ def test_config4_blr_evidence_and_gradient(gpu_lib):
     assert reason & 4, reason  # terminated by dlogZ
     lz_true, g_true = blr_log_evidence(Phi, y, 0.0, np.log(0.5))
     assert abs(res.log_Z_mean - lz_true) < 4 * res.log_Z_uncert + 0.05, (res.log_Z_mean, res.log_Z_uncert, lz_true)
-    out = evidence_and_grad(DeadSet.from_results(res, Phi, y), 0.0, np.log(0.5)).cpu().numpy()
+    ds = DeadSet.from_results(res, Phi, y)
+    out = evidence_and_grad(ds, 0.0, np.log(0.5)).cpu().numpy()
+    se, ess = _gradient_standard_error(ds, 0.0, np.log(0.5))
     rel = np.abs(out[1:] - g_true) / np.abs(g_true)
     print("config4 log Z", res.log_Z_mean, "+-", res.log_Z_uncert, "truth", lz_true, "grad", out[1:], "truth",
-          g_true, "rel", rel)
-    assert np.all(rel < 0.1)
+          g_true, "rel", rel, "standard error", se, "ESS", ess)
+    assert np.all(np.abs(out[1:] - g_true) < 5 * se + 1e-3 * np.abs(g_true)), (out[1:], g_true, se)
+
+
+def _adjoint_scratch(entry, U, log_w, Phi, y, log_tau, log_sigma):
+    """Call one adjoint entry point and return (out, per-point sum r^2, per-point sum r y)."""
+    import ctypes
+    from jaxns_gb300 import _ffi
+    dev = "cuda"
+    t = lambda a, dt: torch.tensor(np.ascontiguousarray(a), dtype=dt, device=dev)
+    Ud, lw, Pd, yd = t(U, torch.float32), t(log_w, torch.float64), t(Phi, torch.float32), t(y, torch.float32)
+    M, P = U.shape
+    N = Phi.shape[0]
+    out = torch.zeros(3, dtype=torch.float64, device=dev)
+    ss = torch.zeros(M, dtype=torch.float64, device=dev)
+    ry = torch.zeros(M, dtype=torch.float64, device=dev)
+    p = lambda a: ctypes.c_void_p(a.data_ptr())
+    args = [p(Ud), p(lw), ctypes.c_longlong(M), ctypes.c_int(P), p(Pd), p(yd), ctypes.c_int(N),
+            ctypes.c_double(log_tau), ctypes.c_double(log_sigma), p(out), p(ss), p(ry)]
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    if entry == "tc":
+        ld = 32 if P <= 32 else 64
+        ws = torch.empty(2 * M * ld, dtype=torch.float32, device=dev)
+        ps = torch.empty(2 * N * ld, dtype=torch.float32, device=dev)
+        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        _ffi.call("gbns_evidence_adjoint_tc", *args, p(ws), p(ps), p(status), stream)
+        assert int(status.item()) == 0
+    else:
+        _ffi.call("gbns_evidence_adjoint", *args, stream)
+    torch.cuda.synchronize()
+    return out.cpu().numpy(), ss.cpu().numpy(), ry.cpu().numpy()
+
+
+@pytest.mark.parametrize("P,N,M", [(8, 300, 100), (32, 4096, 1000), (48, 1000, 777), (64, 700, 3000),
+                                   (5, 257, 129), (33, 256, 128)])
+def test_tc_residuals_against_fp64(gpu_lib, P, N, M):
+    """The 3xTF32 tcgen05 contraction: per-point sum (y - Phi w)^2 and sum (y - Phi w) y
+    against FP64 numpy on the same fp32 inputs (w = tau ndtri(u) evaluated in FP64), on
+    ragged point / row tiles and one or two K blocks; the CUDA-core path alongside."""
+    from scipy.special import ndtri
+    rng = np.random.default_rng(P * 100003 + N * 7 + M)
+    Phi = rng.standard_normal((N, P)).astype(np.float32)
+    y = (Phi.astype(np.float64) @ rng.standard_normal(P) + 0.5 * rng.standard_normal(N)).astype(np.float32)
+    U = rng.uniform(0.02, 0.98, (M, P)).astype(np.float32)
+    log_w = rng.standard_normal(M)
+    lt = 0.2
+    w = np.exp(lt) * ndtri(U.astype(np.float64))
+    r = y.astype(np.float64)[None, :] - w @ Phi.astype(np.float64).T
+    ss_ref = (r * r).sum(1)
+    ry_ref = r @ y.astype(np.float64)
+    for entry in ("tc", "cuda_core"):
+        _, ss, ry = _adjoint_scratch(entry, U, log_w, Phi, y, lt, np.log(0.5))
+        err = np.abs(ss - ss_ref) / ss_ref
+        assert err.max() < 2e-5, (entry, err.max())
+        assert np.max(np.abs(ry - ry_ref) / (np.abs(ry_ref) + np.sqrt(ss_ref * (y.astype(np.float64) ** 2).sum()))) < 2e-5
+
+
+def test_tc_sampler_shell_matches_cuda_core(gpu_lib):
+    """One lock-step shell of a batch of three uneven linear-Gaussian runs (P = 8, 40, 64;
+    N = 300, 700, 257; several 128-chain and 256-row tiles, one and two K blocks) with the
+    tensor-core residual and with the CUDA-core residual: chain by chain the same."""
+    import ctypes
+    import jaxns_gb300 as gb
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.engine import NSBatch
+    specs = []
+    for i, (P, N, n) in enumerate([(8, 300, 300), (40, 700, 400), (64, 257, 260)]):
+        Phi, y = blr(N, P, seed=10 + i)
+        ns = gb.NestedSampler(blr_model(gb, Phi, y), num_live_points=n, num_slices=2 * P)
+        specs.append(ns.nested_sampler.run_spec(gb.random.PRNGKey(20 + i), ns.normalise_term_cond(None)))
+    outs = []
+    for tc in (True, False):
+        b = NSBatch(specs, lg_tensor_cores=tc)
+        b.init()
+        stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _ffi.call("gbns_lg_shell_begin", ctypes.byref(b._b), ctypes.byref(b._lgb), stream)
+        for _ in range(1000):
+            _ffi.call("gbns_lg_steps", ctypes.byref(b._b), ctypes.byref(b._lgb), 16, stream)
+            if int(b.lg_t["chains_left"].sum().item()) == 0:
+                break
+        torch.cuda.synchronize()
+        assert int(b.lg_t["chains_left"].sum().item()) == 0
+        st = b.state()
+        assert np.all(st["status"] == 0), st["status"]
+        outs.append((b.new_U.cpu().numpy().copy(), b.new_E.cpu().numpy().copy(), b.new_L.cpu().numpy().copy()))
+    (U1, E1, L1), (U2, E2, L2) = outs
+    nc = sum(s.shell_size for s in specs)
+    same_E = E1[:nc] == E2[:nc]
+    assert same_E.mean() >= 0.95, same_E.mean()
+    np.testing.assert_allclose(L1[:nc][same_E], L2[:nc][same_E], rtol=1e-4, atol=2e-2)
