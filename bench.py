@@ -10,6 +10,14 @@ to termination plus the device results pass (tree counts, FP64 evidence).
 --workload config3: 4096 independent correlated-Gaussian runs, D ~ U{2..64}, n = 50 D,
 num_slices = 5 D, Sigma = A A^T / D + 0.1 I, prior U[-10,10]^D, dlogZ < 1e-4.
 
+--workload blr: Bayesian linear regression evidence and gradient, Phi in R^{4096x32} ~ N(0,1),
+w ~ N(0, I), y = Phi w + eps (sigma = 0.5), prior w ~ N(0, tau^2 I), (log tau, log sigma) =
+(0, log 0.5), 1024 live points.  --workload blr_batch: 256 such problems with N ~ U[512, 16384],
+P ~ U[8, 64], sigma ~ U[0.1, 1], tau ~ U[0.5, 2], 25 P live points.  One step = every problem's
+nested-sampling run (lock-step slice sampler, tcgen05 Phi w residuals) + the reweighted-evidence
+adjoint (log Z and d log Z / d(log tau, log sigma)); compared against the plain single-run GPU
+loop plus central finite differences (h = 1e-3, four more runs per problem).
+
 All inputs are seeded synthetic data.  The sample stores exceed L2 (no flush needed).
 Metric: NS runs/s of the whole batch, likelihood evaluations/s alongside.
 
@@ -202,16 +210,20 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbns", choices=["gbns", "reference"])
-    ap.add_argument("--workload", default="shells", choices=["shells", "config3"])
+    ap.add_argument("--workload", default="shells", choices=["shells", "config3", "blr", "blr_batch"])
     ap.add_argument("--runs", type=int, default=None)
     ap.add_argument("--block", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--only-dim", type=int, default=None,
                     help="config3: keep only runs of this dimension (repeated to --runs); for kernel profiling")
+    ap.add_argument("--plain-problems", type=int, default=4,
+                    help="blr workloads: problems in the plain GPU + finite-difference comparison")
     ap.add_argument("--iterations", type=int, default=None,
                     help="time init + this many NS iterations instead of whole runs (kernel profiling)")
     args = ap.parse_args()
+    if args.workload in ("blr", "blr_batch"):
+        return main_blr(args)
     if args.runs is None:
         args.runs = 1024 if args.workload == "shells" else 4096
 
@@ -397,6 +409,290 @@ def main():
         v, info = cpu_runs_per_s(wl, args.workload, threads)
         line["cpu_baseline"] = {"value": v, "unit": "runs/s", "cores": threads, "kind": "port",
                                 "sample": info["sample"]}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+# ----------------------------------------------------------------- linear-Gaussian workloads
+
+def blr_information(Phi, y, sigma, tau):
+    """KL(posterior || prior) of w for y ~ N(Phi w, sigma^2 I), w ~ N(0, tau^2 I) (FP64)."""
+    P = Phi.shape[1]
+    A = np.eye(P) / tau ** 2 + Phi.T @ Phi / sigma ** 2
+    S = np.linalg.inv(A)
+    mu = S @ (Phi.T @ y) / sigma ** 2
+    return 0.5 * (np.trace(S) / tau ** 2 + mu @ mu / tau ** 2 - P + P * np.log(tau ** 2) - np.linalg.slogdet(S)[1])
+
+
+def blr_workload(R: int, seed: int, name: str):
+    """Seeded linear-regression evidence problems.  blr: R copies of the 4096 x 32 problem
+    (different data per copy); blr_batch: R problems of uneven size.  The sample store of each
+    is sized from its information content H: n (1.3 H + 2 P + 60)."""
+    if name == "blr":
+        dims = [(4096, 32, 0.5, 1.0)] * R
+    else:
+        rng = np.random.default_rng(seed)
+        dims = list(zip(rng.integers(512, 16385, size=R), rng.integers(8, 65, size=R), rng.uniform(0.1, 1.0, R),
+                        rng.uniform(0.5, 2.0, R)))
+    out = []
+    for r, (N, P, sigma, tau) in enumerate(dims):
+        N, P = int(N), int(P)
+        g = np.random.default_rng([seed, r])
+        Phi = g.standard_normal((N, P)).astype(np.float32)
+        y = (Phi.astype(np.float64) @ g.standard_normal(P) + sigma * g.standard_normal(N)).astype(np.float32)
+        n = 1024 if name == "blr" else 25 * P
+        H = float(blr_information(Phi.astype(np.float64), y.astype(np.float64), sigma, tau))
+        out.append(dict(N=N, P=P, sigma=float(sigma), tau=float(tau), Phi=Phi, y=y, n=n,
+                        cap=int(n * (1.3 * H + 2 * P + 60)), H=H))
+    return out
+
+
+def blr_sampler(p, dlt: float = 0.0, dls: float = 0.0):
+    """NestedSampler of one problem at (log tau + dlt, log sigma + dls), jaxns defaults
+    (num_slices = 5 P, shell = n / 2, default termination)."""
+    import jaxns_gb300 as gb
+    P = p["P"]
+    tau, sigma = p["tau"] * np.exp(dlt), p["sigma"] * np.exp(dls)
+
+    def prior_model():
+        w = yield gb.Prior(gb.Normal(np.zeros(P), tau * np.ones(P)), name="w")
+        return w
+
+    model = gb.Model(prior_model, gb.LinearGaussianLikelihood(p["Phi"], p["y"], sigma))
+    return gb.NestedSampler(model, num_live_points=p["n"], max_samples=p["cap"])
+
+
+def blr_gradient_se(b, res, wl, thetas):
+    """Monte Carlo standard error of each run's reweighted gradient: weighted spread of the
+    per-point d log L / d theta over the Kish effective sample size (fp32 torch, no TF32)."""
+    import torch
+    torch.backends.cuda.matmul.allow_tf32 = False
+    st = b.state()
+    se = np.zeros((len(wl), 2))
+    for r, p in enumerate(wl):
+        M = int(min(st["num_samples"][r], b.specs[r].max_samples))
+        o, uo, P, N = int(b.offsets["store"][r]), int(b.offsets["ustore"][r]), p["P"], p["N"]
+        U = res["U_sorted"][uo:uo + 2 * M * P].view(torch.float64).view(M, P)
+        log_w = (res["log_dp_mean"][o:o + M] - res["log_L_samples"][o:o + M] + res["scalars"][r, 0])
+        Phi = torch.as_tensor(p["Phi"], device=U.device)
+        y = torch.as_tensor(p["y"], device=U.device)
+        tau, s2 = np.exp(thetas[r, 0]), np.exp(2 * thetas[r, 1])
+        ss, rp = [], []
+        for i0 in range(0, M, 16384):
+            w = (tau * np.sqrt(2.0) * torch.erfinv(2.0 * U[i0:i0 + 16384] - 1.0)).float()
+            Pw = w @ Phi.T
+            rr = y[None, :] - Pw
+            ss.append((rr * rr).sum(1).double())
+            rp.append((rr * Pw).sum(1).double())
+        ss, rp = torch.cat(ss), torch.cat(rp)
+        g = torch.stack([rp / s2, ss / s2 - N], 1)
+        pw = torch.softmax(-0.5 * ss / s2 + log_w, 0)
+        mean = (pw[:, None] * g).sum(0)
+        var = (pw[:, None] * (g - mean) ** 2).sum(0)
+        se[r] = torch.sqrt(var * (pw * pw).sum()).cpu().numpy()
+    return se
+
+
+def main_blr(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    name = args.workload
+    if args.runs is None:
+        args.runs = 1 if name == "blr" else 256
+    threads = os.cpu_count() or 1
+    wdesc = ("configs[3] Bayesian linear regression: Phi 4096x32 ~ N(0,1), w ~ N(0,I), sigma=0.5, tau=1, 1024 live "
+             "points, num_slices=5P, default termination; NS run + reweighted-evidence adjoint" if name == "blr" else
+             f"configs[4] batched linear-regression evidence: {args.runs} problems per GPU, N~U[512,16384], "
+             f"P~U[8,64], sigma~U[0.1,1], tau~U[0.5,2], 25P live points, num_slices=5P; NS runs + adjoints")
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the FP64 CPU restatement needs hours per "
+                              "linear-regression problem at these sizes; the GPU line carries a cost-model "
+                              "cpu_baseline (per-evaluation oracle time x the run's evaluation count)"}))
+        return
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    from jaxns_gb300.build import build_library
+    build_library()
+    import jaxns_gb300 as gb
+    from jaxns_gb300.adjoint import batch_evidence_and_grad, blr_log_evidence
+    from jaxns_gb300.batched import BatchedNestedSampler
+    from jaxns_gb300.engine import NSBatch
+
+    wl = blr_workload(args.runs, 2024 + rank, name)
+    R = len(wl)
+    keys = np.array([gb.random.PRNGKey(r) for r in range(R)])
+    bns = BatchedNestedSampler([blr_sampler(p) for p in wl], keys, None, store_U=True)
+    b = bns.batch
+    thetas = np.array([[np.log(p["tau"]), np.log(p["sigma"])] for p in wl])
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def step(from_host=False, max_iterations=None):
+        h2d = b.upload_params() if from_host else 0
+        bns(from_host=from_host, max_iterations=max_iterations, check=max_iterations is None)
+        res = b.results(with_U=True)
+        adj = batch_evidence_and_grad(b, res, thetas, check=max_iterations is None)
+        out = torch.cat([res["scalars"][:, :2], adj], 1)  # [R, 5]: log Z, uncert, log Z(theta), grads
+        if from_host:
+            return out.cpu().numpy(), h2d + int(b.t_state.numel())
+        return out, res
+
+    for _ in range(args.warmup):  # graphs, kernels, result buffers: init + 2 iterations + adjoint
+        step(max_iterations=2)
+    barrier()
+    launches0 = b.kernel_launches
+    with ClockSampler(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        nevals = 0
+        for _ in range(args.steps):
+            out, res = step()
+            nevals += int(b.state()["num_likelihood_evaluations"].sum())
+        ev1.record()
+        barrier()
+    ms = ev0.elapsed_time(ev1)
+    gpu_launches = b.kernel_launches - launches0
+    st = b.state()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = R * args.steps * world / (ms / 1e3)
+    Ns = np.array([p["N"] for p in wl], np.float64)
+    Ps = np.array([p["P"] for p in wl], np.float64)
+    evals = st["num_likelihood_evaluations"].astype(np.float64)
+
+    # accuracy against the analytic evidence and gradient (FP64, on the fp32 inputs)
+    host = out.cpu().numpy()
+    se = blr_gradient_se(b, res, wl, thetas)
+    truth = [blr_log_evidence(p["Phi"].astype(np.float64), p["y"].astype(np.float64), np.log(p["tau"]),
+                              np.log(p["sigma"])) for p in wl]
+    lz_true = np.array([t[0] for t in truth])
+    g_true = np.array([t[1] for t in truth])
+    dz = host[:, 0] - lz_true
+    gerr = host[:, 3:5] - g_true
+    accuracy = {"truth": "analytic BLR evidence and gradient (FP64)", "mean_abs_dlogZ": float(np.mean(np.abs(dz))),
+                "frac_abs_dlogZ_lt_0.1": float(np.mean(np.abs(dz) < 0.1)),
+                "frac_within_3sigma": float(np.mean(np.abs(dz) < 3 * host[:, 1])),
+                "mean_log_Z_uncert": float(np.mean(host[:, 1])),
+                "reweighted_log_Z_minus_run_log_Z_max": float(np.max(np.abs(host[:, 2] - host[:, 0]))),
+                "grad_rel_err_median": [float(v) for v in np.median(np.abs(gerr) / np.abs(g_true), 0)],
+                "grad_err_over_mc_se_median": [float(v) for v in np.median(np.abs(gerr) / se, 0)],
+                "frac_grad_within_3se": [float(v) for v in np.mean(np.abs(gerr) < 3 * se, 0)],
+                "worst_dlogZ": [{"problem": int(r), "N": wl[r]["N"], "P": wl[r]["P"], "sigma": round(wl[r]["sigma"], 3),
+                                 "tau": round(wl[r]["tau"], 3), "H": round(wl[r]["H"], 1), "dlogZ": float(dz[r]),
+                                 "uncert": float(host[r, 1]), "reason": int(st["termination_reason"][r]),
+                                 "samples": int(st["num_samples"][r]), "cap": int(b.specs[r].max_samples)}
+                                for r in np.argsort(-np.abs(dz))[:3]]}
+
+    # residual-kernel roofline: events inside the lock-step graph around every residual launch
+    # over the first iterations of a fresh pass; algorithmic flops 2 N P per evaluation
+    T = args.iterations or 6
+    b.timing = True
+    b.resid_ms, b.resid_launches = 0.0, 0
+    b.reset()
+    b.init()
+    e0 = b.state()["num_likelihood_evaluations"].astype(np.float64)
+    for _ in range(T):
+        b._lg_iteration(use_graph=True)
+    e1 = b.state()["num_likelihood_evaluations"].astype(np.float64)
+    b.timing = False
+    rflops = float(np.sum((e1 - e0) * Ns * Ps * 2.0))
+    achieved = rflops / (b.resid_ms / 1e3) / 1e12 if b.resid_ms > 0 else None
+    peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+        os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
+    peak = float(peaks["bf16_tflops"])
+    roofline = {"bound": "tensor", "kernel": "k_lg_resid_tc (3xTF32 tcgen05 Phi w residuals)", "achieved": achieved,
+                "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if achieved else None, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (dense bf16, burst); dense TF32 issues at half that "
+                               "rate and 3xTF32 issues three MMAs per algorithmic product, so the ceiling of this "
+                               "formulation is peak/6",
+                "frac_of_3xtf32_ceiling": achieved / (peak / 6.0) if achieved else None,
+                "flops": "algorithmic 2 N P per likelihood evaluation (proposal x all data rows)",
+                "timed_iterations": T, "residual_launches": b.resid_launches,
+                "residual_ms": b.resid_ms}
+
+    # end-to-end: Phi, y, sigma and the run table from pinned host memory, per-problem
+    # (log Z, uncertainty, log Z(theta), gradient) back to the host
+    barrier()
+    e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0_.record()
+    for _ in range(args.steps):
+        host_out, h2d = step(from_host=True)
+    e1_.record()
+    barrier()
+    e2e_ms = e0_.elapsed_time(e1_)
+    e2e = {"value": R * args.steps * world / (e2e_ms / 1e3), "unit": "problems/s", "h2d_bytes_per_step": h2d,
+           "d2h_bytes_per_step": int(R * 5 * 8)}
+
+    line = {"metric": METRIC, "value": value, "unit": "problems/s (NS run + adjoint)", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (3xTF32 tensor-core residuals, FP64 evidence)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": wdesc, "problems_per_gpu": R, "warmup_steps": "init + 2 iterations + adjoint",
+                       "l2": "per-step sample stores > L2 (no flush needed)"},
+            "likelihood_evals_per_s": nevals * world / (ms / 1e3), "gpu_launches": int(gpu_launches),
+            "roofline": roofline, "e2e": e2e, "clocks": clk.summary(), "accuracy": accuracy,
+            "iterations": {"max": int(st["iterations"].max()), "mean": float(st["iterations"].mean())},
+            "information_H": {"min": float(min(p["H"] for p in wl)), "max": float(max(p["H"] for p in wl))}}
+
+    if rank == 0 and not args.no_plain:
+        # plain GPU path + finite differences: problems one at a time, eager launches, five
+        # runs each (theta, log tau +- h, log sigma +- h), no adjoint
+        h = 1e-3
+        # the plain path takes ~5x the batched work one problem at a time, so it is sampled on
+        # the cheapest problems (by evaluations x N x P): its problems/s is then an upper
+        # bound and the fused speed-up a lower bound
+        cost = evals * Ns * Ps
+        idx = sorted(np.argsort(cost)[:min(args.plain_problems, R)].tolist())
+        tot, fd = 0.0, []
+        for r in idx:
+            lz = []
+            for dlt, dls in [(0, 0), (h, 0), (-h, 0), (0, h), (0, -h)]:
+                ns = blr_sampler(wl[r], dlt, dls)
+                one = NSBatch([ns.nested_sampler.run_spec(keys[r], ns.normalise_term_cond(None))])
+                torch.cuda.synchronize()
+                t0 = time.time()
+                one.run(use_graph=False)
+                sc = one.results(with_U=False)["scalars"].cpu().numpy()
+                tot += time.time() - t0
+                lz.append(float(sc[0, 0]))
+                del one
+            fd.append([(lz[1] - lz[2]) / (2 * h), (lz[3] - lz[4]) / (2 * h)])
+        fd = np.array(fd)
+        plain = len(idx) / tot
+        line["plain_gpu_plus_fd"] = {"problems_per_s": plain, "sample": f"problems {idx} (the cheapest by evaluations x "
+                                     "N x P), 5 eager single-problem runs each", "fused_speedup": value / world / plain,
+                                     "fd_grad_rel_err_median": [float(v) for v in np.median(
+                                         np.abs(fd - g_true[idx]) / np.abs(g_true[idx]), 0)]}
+    if rank == 0 and not args.no_cpu:
+        from oracle import oracle
+        oracle.build()
+        idx = list(range(0, R, max(1, R // 16)))
+        per = []
+        for r in idx:
+            p = wl[r]
+            om = oracle.lingauss_model(p["Phi"].astype(np.float64), p["y"].astype(np.float64), p["sigma"], p["tau"])
+            U = np.random.default_rng(r).uniform(0.05, 0.95, size=(64, p["P"]))
+            t0 = time.time()
+            oracle.forward(om, U)
+            per.append((time.time() - t0) / 64 * evals[r])
+        cpu_s = float(np.mean(per)) * R / threads
+        line["cpu_baseline"] = {"value": R / cpu_s, "unit": "problems/s", "cores": threads, "kind": "port",
+                                "sample": f"cost model: FP64 oracle likelihood time per evaluation (64 points) on "
+                                          f"problems {idx}, x each problem's evaluation count in this run, "
+                                          f"spread over {threads} host threads (NS overhead and adjoint excluded)"}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

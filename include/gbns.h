@@ -90,7 +90,9 @@ typedef struct {
     int midpoint;     /* midpoint_shrink */
     int uniform_phase;/* 1: run the UniformSampler phase first (init_efficiency_threshold > 0) */
     int N;            /* rows of Phi (linear-Gaussian family) */
-    int pad0;
+    int ucols;      /* 32-bit words of U storage per point: D (fp32 U), or 2 D for the
+                       linear-Gaussian family, whose U is FP64 (the Normal prior's tails need
+                       it; stored as D doubles in the same float buffers) */
     double init_efficiency_threshold;
     double log_L_offset;   /* FP64 constant part of log L; device values are log L - log_L_offset */
     long long cap;         /* store capacity (max_samples, rounded) */
@@ -177,9 +179,11 @@ typedef struct {
  * indexed like the shell outputs ([sum s] and [sum s * D]). */
 typedef struct {
     int *j, *in_slice, *total, *flags;      /* [sum s] */
-    float *left, *right, *t, *alpha, *logL0; /* [sum s] */
+    double *left, *right, *t, *alpha;       /* [sum s] slice interval, point, shrink factor (U space, FP64) */
+    float *logL0;                           /* [sum s] */
     uint32_t *ck, *after_key, *slices_key, *dir_key; /* [sum s * 2] */
-    float *u0, *dir, *W;                    /* [sum s * D]: seed point, direction, proposal w */
+    double *u0, *dir;                       /* [sum s * D]: seed point and direction (U space, FP64) */
+    float *W;                               /* [sum s * D]: proposal w (CUDA-core residual path) */
     double *ss;                             /* [sum s] residual sums of the pending proposals */
     int *chains_left;                       /* [R] chains of the current shell not yet finished */
     const int *items;                       /* [num_items * 4]: (run, first chain, chain count, first data row) */
@@ -228,7 +232,8 @@ int gbns_random_bits64(const uint32_t *key_dev, uint64_t *out_dev, long long n, 
 int gbns_uniform(const uint32_t *key_dev, float *out_dev, long long n, void *stream);
 int gbns_normal(const uint32_t *key_dev, float *out_dev, long long n, void *stream);
 
-/* Model.forward over B points of one run's model: U [B, D] -> log L [B] */
+/* Model.forward over B points of one run's model: U [B, ucols] words -> log L [B]
+ * (fp32 U [B, D], or FP64 U [B, D] for the linear-Gaussian family) */
 int gbns_forward(const gbns_batch *batch, int run, const float *U_dev, float *logL_dev, long long B,
                  void *stream);
 
@@ -273,6 +278,10 @@ int gbns_count_crossed_edges_static(const int *sender_dev, const float *log_L_de
  *      uni_slice_sampler.py:343-441) for a likelihood evaluated in batches */
 int gbns_lg_shell_begin(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps, void *stream);
+/* The two halves of one gbns_lg_steps step: the chain step (consume the pending residuals,
+ * propose the next point) and the residual contraction of all pending proposals. */
+int gbns_lg_chain_step(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
+int gbns_lg_residual(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 /* Split each run's Phi (fparams) into the TF32 hi/lo row-padded copies lg->Phi_hi / Phi_lo
  * used by the tensor-core residual path.  Call once per batch, before the first step. */
 int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
@@ -281,15 +290,16 @@ int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *st
  * (experimental/evidence_maximisation.py:151-160, weights :213):
  *   log Z(theta) = logsumexp_i(log L_theta(U_i) + log_w_i),  w_i = tau * ndtri(U_i),
  *   out[0] = log Z(theta), out[1] = d/d log tau, out[2] = d/d log sigma  (FP64 reductions).
- * Per-point residuals are recomputed from U, never stored.  ss_scratch, ry_scratch: [M]. */
-int gbns_evidence_adjoint(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+ * Per-point residuals are recomputed from U [M, P] (FP64), never stored.  ss_scratch,
+ * ry_scratch: [M]. */
+int gbns_evidence_adjoint(const double *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
                           const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
                           double *ss_scratch_dev, double *ry_scratch_dev, void *stream);
 /* The same on the tcgen05 tensor cores (3xTF32 contraction).  Extra scratch, with
  * ld = 32 for P <= 32 and 64 otherwise: w_scratch [2 * M * ld] floats, phi_scratch
  * [2 * N * ld] floats; status_dev: one int, GBNS_ERR_WAIT_TIMEOUT is or-ed in if a wait of
  * the kernel timed out (the outputs are then invalid).  M < 2^31. */
-int gbns_evidence_adjoint_tc(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+int gbns_evidence_adjoint_tc(const double *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
                              const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
                              double *ss_scratch_dev, double *ry_scratch_dev, float *w_scratch_dev,
                              float *phi_scratch_dev, int *status_dev, void *stream);

@@ -35,7 +35,7 @@ class EvCalc(ctypes.Structure):
 
 class RunDesc(ctypes.Structure):
     _fields_ = [("D", c_int), ("n", c_int), ("s", c_int), ("S", c_int), ("K", c_int), ("family", c_int),
-                ("midpoint", c_int), ("uniform_phase", c_int), ("N", c_int), ("pad0", c_int),
+                ("midpoint", c_int), ("uniform_phase", c_int), ("N", c_int), ("ucols", c_int),
                 ("init_efficiency_threshold", c_double), ("log_L_offset", c_double), ("cap", c_ll), ("live_off", c_ll),
                 ("store_off", c_ll), ("shell_off", c_ll), ("param_off", c_ll), ("prior_off", c_ll),
                 ("ustore_off", c_ll), ("liveU_off", c_ll), ("newU_off", c_ll), ("phU_off", c_ll),
@@ -85,7 +85,7 @@ EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2
             "gbns_batch_finalize", "gbns_batch_results", "gbns_slice_shell", "gbns_count_crossed_edges",
             "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
             "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint",
-            "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc")
+            "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc", "gbns_lg_chain_step", "gbns_lg_residual")
 
 _lib = None
 

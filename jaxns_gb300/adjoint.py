@@ -22,7 +22,7 @@ from . import _ffi
 @dataclass
 class DeadSet:
     """The fixed dead points of one run (device tensors)."""
-    U: torch.Tensor        # [M, P] float32
+    U: torch.Tensor        # [M, P] float64 (U space)
     log_w: torch.Tensor    # [M] float64
     Phi: torch.Tensor      # [N, P] float32
     y: torch.Tensor        # [N] float32
@@ -31,7 +31,7 @@ class DeadSet:
     def from_results(results, Phi, y) -> "DeadSet":
         log_w = (results.log_dp_mean - results.log_L_samples + results.log_Z_mean).contiguous()
         dev = results.U_samples.device
-        return DeadSet(U=results.U_samples.contiguous(), log_w=log_w.to(torch.float64),
+        return DeadSet(U=results.U_samples.to(torch.float64).contiguous(), log_w=log_w.to(torch.float64),
                        Phi=torch.as_tensor(np.asarray(Phi, np.float32), device=dev).contiguous(),
                        y=torch.as_tensor(np.asarray(y, np.float32), device=dev).contiguous())
 
@@ -61,6 +61,53 @@ def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float, tensor_core
     status = torch.zeros(1, dtype=torch.int32, device=dev)
     _ffi.call("gbns_evidence_adjoint_tc", *args, p(ws), p(ps), p(status), stream)
     if check and int(status.item()) != 0:
+        raise _ffi.GBNSError(f"gbns_evidence_adjoint_tc: device status {int(status.item())} (wait timed out)")
+    return out
+
+
+def batch_evidence_and_grad(batch, results, thetas, tensor_cores: bool = True, check: bool = True):
+    """Reweighted evidence and gradient of every linear-Gaussian run of an NSBatch from one
+    device results pass (NSBatch.results(with_U=True)); thetas: [R, 2] (log tau, log sigma).
+    Phi and y are read in place from the batch's parameter buffer.  Returns [R, 3] FP64 on
+    the device: log Z(theta), d/d log tau, d/d log sigma."""
+    st = batch.state()
+    R = batch.R
+    dev = batch.device
+    out = torch.zeros(R, 3, dtype=torch.float64, device=dev)
+    sizes = []
+    for r, s in enumerate(batch.specs):
+        sizes.append((int(min(st["num_samples"][r], s.max_samples)), s.D, s.N))
+    Mmax = max(m for m, _, _ in sizes)
+    Nmax = max(n for _, _, n in sizes)
+    ss = torch.empty(max(Mmax, 1), dtype=torch.float64, device=dev)
+    ry = torch.empty(max(Mmax, 1), dtype=torch.float64, device=dev)
+    ws = torch.empty(max(2 * Mmax * 64, 1), dtype=torch.float32, device=dev)
+    ps = torch.empty(2 * Nmax * 64, dtype=torch.float32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    log_Z = results["scalars"][:, 0]
+    log_w_all = results["log_dp_mean"] - results["log_L_samples"]
+    thetas = np.asarray(thetas, np.float64).reshape(R, 2)
+    for r, s in enumerate(batch.specs):
+        M, P, N = sizes[r]
+        o = int(batch.offsets["store"][r])
+        uo = int(batch.offsets["ustore"][r])
+        if uo < 0:
+            raise ValueError("the batch was built without a U store (store_U=False)")
+        log_w = (log_w_all[o:o + M] + log_Z[r]).contiguous()
+        U = results["U_sorted"][uo:uo + 2 * M * P]  # FP64 U as pairs of 32-bit words
+        po = int(batch.offsets["param"][r])
+        Phi = batch.fparams[po:po + N * P]
+        y = batch.fparams[po + N * P:po + N * P + N]
+        args = [p(U), p(log_w), ctypes.c_longlong(M), ctypes.c_int(P), p(Phi), p(y), ctypes.c_int(N),
+                ctypes.c_double(thetas[r, 0]), ctypes.c_double(thetas[r, 1]), p(out[r]), p(ss), p(ry)]
+        if tensor_cores:
+            _ffi.call("gbns_evidence_adjoint_tc", *args, p(ws), p(ps), p(status), stream)
+        else:
+            _ffi.call("gbns_evidence_adjoint", *args, stream)
+        batch.kernel_launches += 5 if tensor_cores else 2
+    if check and tensor_cores and int(status.item()) != 0:
         raise _ffi.GBNSError(f"gbns_evidence_adjoint_tc: device status {int(status.item())} (wait timed out)")
     return out
 

@@ -18,7 +18,7 @@ from .public import NestedSampler, NestedSamplerResults, TerminationCondition, r
 
 class BatchedNestedSampler:
     def __init__(self, samplers: Sequence[NestedSampler], keys, term_conds: Optional[Sequence] = None,
-                 block: int = 16, chains_per_item: int = 64, store_U: bool = False):
+                 block: int = 16, chains_per_item: int = 64, store_U: bool = False, lg_tensor_cores: bool = True):
         self.samplers = list(samplers)
         keys = np.asarray(keys, np.uint32).reshape(len(self.samplers), 2)
         if term_conds is None:
@@ -29,13 +29,15 @@ class BatchedNestedSampler:
             spec.store_U = store_U
             specs.append(spec)
         self.block = int(block)
-        self.batch = NSBatch(specs, chains_per_item=chains_per_item)
+        self.batch = NSBatch(specs, chains_per_item=chains_per_item, lg_tensor_cores=lg_tensor_cores)
         self.state = None
 
-    def __call__(self, from_host: bool = True, use_graph: bool = True, check: bool = True):
-        """Run every problem to termination.  Returns the termination reasons (host)."""
+    def __call__(self, from_host: bool = True, use_graph: bool = True, check: bool = True,
+                 max_iterations: Optional[int] = None):
+        """Run every problem to termination (or max_iterations).  Returns the termination
+        reasons (host)."""
         self.batch.reset(from_host=from_host)
-        self.state = self.batch.run(block=self.block, use_graph=use_graph, check=check)
+        self.state = self.batch.run(block=self.block, use_graph=use_graph, check=check, max_iterations=max_iterations)
         return self.state["termination_reason"].astype(np.int64)
 
     def summary(self):

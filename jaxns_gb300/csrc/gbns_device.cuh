@@ -422,10 +422,6 @@ __device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ 
 
 // ------------------------------------------------------------- likelihood ----
 
-// Per-run parameter views (fparams layout written by the host, see engine.py):
-//  MVN:     [mu(D), Linv(D*D row-major, lower), c0]   c0 = -sum log L_ii - D/2 log 2pi
-//  SHELLS:  [c1(D), c2(D), R, w, norm]                 norm = log sqrt(2 pi w^2)
-//  LINGAUSS:[Phi(N*D row-major), y(N), sigma]
 // x = hi + lo with hi and lo both TF32 (round to nearest, ties away): the operand split of
 // the 3xTF32 tensor-core contraction (hi*hi + hi*lo + lo*hi).
 __device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
@@ -436,9 +432,34 @@ __device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
   lo = __uint_as_float(l);
 }
 
+// Standard-normal quantile of an FP64 u, evaluated in fp32 without losing the tails: the
+// argument handed to the fp32 inverse is formed exactly in FP64 (2u - 1 near the centre,
+// 2u or 2 - 2u in the tails), so u within 1e-12 of 0 or 1 still maps to its own quantile.
+__device__ __forceinline__ float ndtri_from_double(double u) {
+  const double z = 2.0 * u - 1.0;
+  if (fabs(z) < 0.5) return GBNS_SQRT2F * erfinvf((float)z);
+  return u < 0.5 ? -GBNS_SQRT2F * erfcinvf((float)(2.0 * u)) : GBNS_SQRT2F * erfcinvf((float)(2.0 - 2.0 * u));
+}
+
+// jax.random.uniform in FP64: the top 52 bits as the mantissa of [1, 2), minus 1.
+__device__ __forceinline__ double uniform01_d(uint64_t bits) {
+  return (double)(bits >> 12) * 2.220446049250313e-16;
+}
+
+// Per-run parameter views (fparams layout written by the host, see engine.py):
+//  MVN:     [mu(D), Linv(D*D row-major, lower), c0]   c0 = -sum log L_ii - D/2 log 2pi
+//  SHELLS:  [c1(D), c2(D), R, w, norm]                 norm = log sqrt(2 pi w^2)
+//  LINGAUSS:[Phi(N*D row-major), y(N), sigma]
+// Prior quantiles: Uniform a + b u (b = high - low), Normal a + b ndtri(u) (b = scale).
 __device__ __forceinline__ float prior_quantile(int kind, float a, float b, float u) {
   if (kind == GBNS_PRIOR_UNIFORM) return fmaf(b, u, a);
   return fmaf(b, GBNS_SQRT2F * erfinvf(fmaf(2.0f, u, -1.0f)), a);
+}
+
+// The same of an FP64 u (the linear-Gaussian family's U space).
+__device__ __forceinline__ float prior_quantile_d(int kind, float a, float b, double u) {
+  if (kind == GBNS_PRIOR_UNIFORM) return (float)((double)a + (double)b * u);
+  return fmaf(b, ndtri_from_double(u), a);
 }
 
 }  // namespace gbns

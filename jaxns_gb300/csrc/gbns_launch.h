@@ -5,6 +5,9 @@
 
 namespace gbns {
 
+// Lock-step chain flags of the linear-Gaussian sampler (gbns_lg_bufs.flags).
+enum : int { LG_START = 1, LG_NEED_DIR = 2, LG_PENDING = 4, LG_FAILED = 8, LG_DONE = 16 };
+
 cudaError_t launch_slice_shells(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
 cudaError_t launch_slice_warp(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
 cudaError_t launch_init(const gbns_batch &b, long long total_points, cudaStream_t stream);
@@ -16,12 +19,13 @@ cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long l
                                        int *num_live, long long *scratch_ll, int *scratch_i, cudaStream_t stream);
 cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream);
+cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t stream);
 cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_adjoint_reduce(const double *log_w, long long M, int N, double log_sigma, const double *ss,
                                   const double *ry, double *out, cudaStream_t stream);
-cudaError_t launch_adjoint_tc(const float *U, const double *log_w, long long M, int P, const float *Phi,
+cudaError_t launch_adjoint_tc(const double *U, const double *log_w, long long M, int P, const float *Phi,
                               const float *y, int N, double log_tau, double log_sigma, double *out, double *ss,
                               double *ry, float *w_scratch, float *phi_scratch, int *status, cudaStream_t stream);
 // Sets the thread-local message returned by gbns_last_error().

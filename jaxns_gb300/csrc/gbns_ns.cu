@@ -57,11 +57,34 @@ __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, co
   return (v != v) ? -INFINITY : v;
 }
 
+// Linear-Gaussian log L (relative to the run's offset) of an FP64 U: -|y - Phi w|^2 / (2 sigma^2).
+__device__ float loglik_lg_d(const gbns_batch &b, const gbns_run_desc &rd, const double *U) {
+  const int D = rd.D, N = rd.N;
+  const float *fp = b.fparams + rd.param_off;
+  float x[64];
+  for (int j = 0; j < D; ++j)
+    x[j] = prior_quantile_d(b.prior_kind[rd.prior_off + j], b.prior_a[rd.prior_off + j],
+                            b.prior_b[rd.prior_off + j], U[j]);
+  const float *Phi = fp, *y = fp + (size_t)N * D;
+  const float sigma = fp[(size_t)N * D + N];
+  float ss = 0.f;
+  for (int a = 0; a < N; ++a) {
+    float r = y[a];
+    for (int j = 0; j < D; ++j) r = fmaf(-Phi[(size_t)a * D + j], x[j], r);
+    ss = fmaf(r, r, ss);
+  }
+  const float v = -0.5f * ss / (sigma * sigma);
+  return (v != v) ? -INFINITY : v;
+}
+
+// U: [B, ucols] 32-bit words (FP64 U for the linear-Gaussian family).
 __global__ void k_forward(gbns_batch b, int run, const float *__restrict__ U, float *__restrict__ out, long long B) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= B) return;
   const gbns_run_desc &rd = b.runs[run];
-  out[i] = (float)((double)loglik_generic(b, rd, U + i * rd.D) + rd.log_L_offset);
+  const float v = rd.family == GBNS_LIK_LINGAUSS ? loglik_lg_d(b, rd, (const double *)U + i * rd.D)
+                                                 : loglik_generic(b, rd, U + i * rd.D);
+  out[i] = (float)((double)v + rd.log_L_offset);
 }
 
 // ------------------------------------------------------------ termination ----
@@ -149,7 +172,7 @@ __device__ void store_append(const gbns_batch &b, const gbns_run_desc &rd, long 
   long long start = nsi;
   if (start > rd.cap - cnt) start = rd.cap - cnt;
   if (start < 0) start = 0;
-  const int D = rd.D;
+  const int W = rd.ucols;
   for (long long i = threadIdx.x; i < cnt; i += blockDim.x) {
     const long long o = rd.store_off + start + i;
     b.store_L[o] = L[i];
@@ -158,8 +181,8 @@ __device__ void store_append(const gbns_batch &b, const gbns_run_desc &rd, long 
     b.store_P[o] = (uint8_t)phantom;
   }
   if (rd.ustore_off >= 0 && b.store_U) {
-    float *dst = b.store_U + rd.ustore_off + (start * D);
-    for (long long q = threadIdx.x; q < cnt * D; q += blockDim.x) dst[q] = U[q];
+    float *dst = b.store_U + rd.ustore_off + (start * W);
+    for (long long q = threadIdx.x; q < cnt * W; q += blockDim.x) dst[q] = U[q];
   }
 }
 
@@ -179,17 +202,24 @@ __global__ void k_init_points(gbns_batch b, long long total) {
   const gbns_run_desc &rd = b.runs[r];
   const int i = (int)(g - rd.live_off);
   const int D = rd.D;
+  const bool lg = rd.family == GBNS_LIK_LINGAUSS;
   const Key K0 = {b.state[r].key[0], b.state[r].key[1]};
   const Key sample_key = fold(K0, 1u);
   const Key ki = fold(sample_key, (uint32_t)i);
   Key k = fold(ki, 0u), sk = fold(ki, 1u);
   float U[64];
+  double Ud[64];
   float logL;
   int ne = 0;
   for (;;) {
     const Key uk = fold(sk, 1u);  // Model.sample_U: uniform(split(key)[1], (D,))
-    for (int j = 0; j < D; ++j) U[j] = uniform01(bits64(uk, (uint32_t)j));
-    logL = loglik_generic(b, rd, U);
+    if (lg) {
+      for (int j = 0; j < D; ++j) Ud[j] = uniform01_d(bits64(uk, (uint32_t)j));
+      logL = loglik_lg_d(b, rd, Ud);
+    } else {
+      for (int j = 0; j < D; ++j) U[j] = uniform01(bits64(uk, (uint32_t)j));
+      logL = loglik_generic(b, rd, U);
+    }
     ++ne;
     if (!(logL <= -INFINITY)) break;
     if (ne >= 1000000) { atomicOr(&b.state[r].status, (int)GBNS_ERR_INIT_BUDGET); break; }
@@ -198,7 +228,12 @@ __global__ void k_init_points(gbns_batch b, long long total) {
     k = nk;
   }
   const long long o = rd.live_off + i;
-  for (int j = 0; j < D; ++j) b.live_U[1][rd.liveU_off + (long long)i * D + j] = U[j];
+  if (lg) {
+    double *dst = (double *)(b.live_U[1] + rd.liveU_off) + (long long)i * D;
+    for (int j = 0; j < D; ++j) dst[j] = Ud[j];
+  } else {
+    for (int j = 0; j < D; ++j) b.live_U[1][rd.liveU_off + (long long)i * D + j] = U[j];
+  }
   b.live_L[1][o] = logL;
   b.live_Lc[1][o] = -INFINITY;
   b.live_E[1][o] = ne;
@@ -212,17 +247,17 @@ __global__ void k_init_finish(gbns_batch b) {
   const int r = blockIdx.x;
   const gbns_run_desc &rd = b.runs[r];
   gbns_run_state &st = b.state[r];
-  const int n = rd.n, D = rd.D;
+  const int n = rd.n, W = rd.ucols;
   int NP = 1;
   while (NP < n) NP <<= 1;
   const float *iL = b.live_L[1] + rd.live_off;
   for (int i = threadIdx.x; i < NP; i += blockDim.x) sk[i] = i < n ? sort_key(iL[i], i) : ~0ull;
   cta_bitonic(sk, NP);
   const long long o = rd.live_off;
-  for (long long q = threadIdx.x; q < (long long)n * D; q += blockDim.x) {
-    const int i = (int)(q / D), j = (int)(q % D);
+  for (long long q = threadIdx.x; q < (long long)n * W; q += blockDim.x) {
+    const int i = (int)(q / W), j = (int)(q % W);
     const int src = (int)(sk[i] & 0xffffffffu);
-    b.live_U[0][rd.liveU_off + (long long)i * D + j] = b.live_U[1][rd.liveU_off + (long long)src * D + j];
+    b.live_U[0][rd.liveU_off + (long long)i * W + j] = b.live_U[1][rd.liveU_off + (long long)src * W + j];
   }
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
     const int src = (int)(sk[i] & 0xffffffffu);
@@ -288,7 +323,7 @@ __global__ void __launch_bounds__(1024) k_merge(gbns_batch b) {
   const gbns_run_desc &rd = b.runs[r];
   gbns_run_state &st = b.state[r];
   if (st.done || st.phase != 1) return;
-  const int n = rd.n, s = rd.s, D = rd.D, K = rd.K;
+  const int n = rd.n, s = rd.s, W = rd.ucols, K = rd.K;
   const int par = st.parity, npar = par ^ 1;
   const long long o = rd.live_off;
   const float *L = b.live_L[par] + o;
@@ -319,10 +354,10 @@ __global__ void __launch_bounds__(1024) k_merge(gbns_batch b) {
   for (int i = threadIdx.x; i < NP; i += blockDim.x)
     sk[i] = i < n ? sort_key(i < s ? nL[i] : L[i], i) : ~0ull;
   cta_bitonic(sk, NP);
-  for (long long q = threadIdx.x; q < (long long)n * D; q += blockDim.x) {
-    const int i = (int)(q / D), j = (int)(q % D);
+  for (long long q = threadIdx.x; q < (long long)n * W; q += blockDim.x) {
+    const int i = (int)(q / W), j = (int)(q % W);
     const int src = (int)(sk[i] & 0xffffffffu);
-    oU[(long long)i * D + j] = src < s ? nU[(long long)src * D + j] : U[(long long)src * D + j];
+    oU[(long long)i * W + j] = src < s ? nU[(long long)src * W + j] : U[(long long)src * W + j];
   }
   long long eloc = 0, enew = 0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {

@@ -6,13 +6,19 @@
 // a shell advance together: gbns_lg_step runs each chain's slice logic up to its next
 // proposal (same RNG stream and decisions as uni_slice_sampler.py:114-273, :343-441), and the
 // residual kernel evaluates |y - Phi w|^2 for all proposals of the step at once.
+//
+// U is FP64 in this family (as in the reference, which runs in f64): with a Normal prior
+// the posterior can sit where u is within 1e-8 of 0 or 1, which fp32 cannot resolve.  The
+// slice arithmetic (seed, direction, bounds, point) is FP64; w = prior quantile is formed
+// in fp32 from an exactly computed tail argument (ndtri_from_double).  FP64 U is kept in
+// the float U buffers as pairs of 32-bit words (gbns_run_desc.ucols = 2 D), so the generic
+// merge / store / results kernels move it unchanged.  Chain-local offsets in doubles are
+// the float offsets halved.
 #include <cstdio>
 #include "gbns_device.cuh"
 #include "gbns_launch.h"
 
 namespace gbns {
-
-enum : int { LG_START = 1, LG_NEED_DIR = 2, LG_PENDING = 4, LG_FAILED = 8, LG_DONE = 16 };
 
 __device__ __forceinline__ int run_of_chain(const gbns_batch &b, long long g) {
   int lo = 0, hi = b.num_runs;
@@ -23,11 +29,12 @@ __device__ __forceinline__ int run_of_chain(const gbns_batch &b, long long g) {
   return lo;
 }
 
-__device__ __forceinline__ float lg_alpha(int j, int S) {
-  if (S == 1) return 0.5f;
-  if (j == S - 1) return 1.0f;
-  const float step = (float)j / (float)(S - 1);
-  return 0.5f * (1.0f - step) + step;
+// linspace(0.5, 1, S)[j] (the midpoint shrink factors, uni_slice_sampler.py:114-273), FP64.
+__device__ __forceinline__ double lg_alpha(int j, int S) {
+  if (S == 1) return 0.5;
+  if (j == S - 1) return 1.0;
+  const double step = (double)j / (double)(S - 1);
+  return __dadd_rn(__dmul_rn(0.5, 1.0 - step), step);
 }
 
 // A chain's first state of the shell: seed point (resample_indicies over log L > L*),
@@ -43,7 +50,7 @@ __global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
   if (c >= rd.s) return;
   const int n = rd.n, P = rd.D;
   const float *liveL = b.live_L[st.parity] + rd.live_off;
-  const float *liveU = b.live_U[st.parity] + rd.liveU_off;
+  const double *liveU = (const double *)(b.live_U[st.parity] + rd.liveU_off);
   const float Lstar = liveL[rd.s - 1];
   int lo = 0, hi = n;
   while (lo < hi) {
@@ -64,7 +71,7 @@ __global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
     if (lo64 & ((1ull << 52) - 1)) kk += 1;
     idx = (n - m) + (int)kk - 1;
   }
-  float *u0 = lg.u0 + rd.newU_off + (size_t)c * P;
+  double *u0 = lg.u0 + (rd.newU_off >> 1) + (size_t)c * P;
   for (int p = 0; p < P; ++p) u0[p] = liveU[(size_t)idx * P + p];
   lg.logL0[g] = liveL[idx];
   const Key dk = fold(chain_key, 0u), sk = fold(chain_key, 1u);
@@ -80,10 +87,13 @@ __global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
   if (c == 0) lg.chains_left[r] = rd.s;
 }
 
+
 // One likelihood evaluation per chain: consume the pending result, then prepare the next
-// proposal w (written to lg.W) or finish the chain.
-__global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains) {
-  const long long g = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+// proposal w or finish the chain.  One warp per chain, lanes over the dimensions
+// (p = lane, lane + 32), so every per-dimension read and write is a coalesced row access.
+__global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains) {
+  const long long g = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
   if (g >= total_chains) return;
   const int r = run_of_chain(b, g);
   const gbns_run_desc &rd = b.runs[r];
@@ -94,23 +104,28 @@ __global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
   int flags = lg.flags[g];
   if (flags & LG_DONE) return;
   const int P = rd.D, S = rd.S, K = rd.K, N = rd.N;
+  const int pa_ = lane, pb_ = lane + 32;
+  const bool ha = pa_ < P, hb = pb_ < P;
   const float *fp = b.fparams + rd.param_off;
   const float sigma = fp[(size_t)N * P + N];
   const float inv2s2 = 0.5f / (sigma * sigma);
   const float Lstar = b.live_L[st.parity][rd.live_off + rd.s - 1];
-  float *u0 = lg.u0 + rd.newU_off + (size_t)c * P;
-  float *d = lg.dir + rd.newU_off + (size_t)c * P;
-  float *W = lg.W + rd.newU_off + (size_t)c * P;
+  const long long du = rd.newU_off >> 1;  // chain vectors in doubles
+  double *u0 = lg.u0 + du + (size_t)c * P;
+  double *d = lg.dir + du + (size_t)c * P;
+  double ua = ha ? u0[pa_] : 0.0, ub = hb ? u0[pb_] : 0.0;
+  double da = ha ? d[pa_] : 0.0, db = hb ? d[pb_] : 0.0;
   int j = lg.j[g], total = lg.total[g], in_slice = lg.in_slice[g];
-  float left = lg.left[g], right = lg.right[g], t = lg.t[g], alpha = lg.alpha[g], logL0 = lg.logL0[g];
+  double left = lg.left[g], right = lg.right[g], t = lg.t[g], alpha = lg.alpha[g];
+  float logL0 = lg.logL0[g];
   Key ck = {lg.ck[2 * g], lg.ck[2 * g + 1]};
   Key after_key = {lg.after_key[2 * g], lg.after_key[2 * g + 1]};
   Key dir_key = {lg.dir_key[2 * g], lg.dir_key[2 * g + 1]};
   const Key slices_key = {lg.slices_key[2 * g], lg.slices_key[2 * g + 1]};
+  bool u_changed = false, d_changed = false;
 
   if (flags & LG_PENDING) {
     const double ss = lg.ss[g];
-    lg.ss[g] = 0.0;
     float logL = (float)(-ss * (double)inv2s2);  // relative to the run's log_L_offset
     if (logL != logL) logL = -INFINITY;
     ++total;
@@ -118,13 +133,16 @@ __global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
     const bool accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
     if (accept || in_slice >= b.max_evals_per_slice) {
       if (!accept) flags |= LG_FAILED;
-      for (int p = 0; p < P; ++p) u0[p] = fmaf(t, d[p], u0[p]);
+      ua = __dadd_rn(ua, __dmul_rn(t, da));
+      ub = __dadd_rn(ub, __dmul_rn(t, db));
+      u_changed = true;
       logL0 = logL;
       const int ph = j - (S - 1 - K);
       if (K > 0 && ph >= 0 && j < S - 1) {
-        float *phU = b.ph_U + rd.phU_off + ((size_t)c * K + ph) * P;
-        for (int p = 0; p < P; ++p) phU[p] = u0[p];
-        b.ph_L[rd.phL_off + (size_t)c * K + ph] = logL;
+        double *phU = (double *)(b.ph_U + rd.phU_off) + ((size_t)c * K + ph) * P;
+        if (ha) phU[pa_] = ua;
+        if (hb) phU[pb_] = ub;
+        if (lane == 0) b.ph_L[rd.phL_off + (size_t)c * K + ph] = logL;
       }
       ++j;
       flags |= LG_START;
@@ -140,26 +158,27 @@ __global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
     flags &= ~LG_PENDING;
   }
   if (flags & LG_DONE) {
-    float *nu = b.new_U + rd.newU_off + (size_t)c * P;
-    for (int p = 0; p < P; ++p) nu[p] = u0[p];
-    b.new_L[rd.shell_off + c] = logL0;
-    b.new_E[rd.shell_off + c] = total;
-    if (flags & LG_FAILED) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
-    atomicSub(&lg.chains_left[r], 1);
+    double *nu = (double *)(b.new_U + rd.newU_off) + (size_t)c * P;
+    if (ha) nu[pa_] = ua;
+    if (hb) nu[pb_] = ub;
+    if (lane == 0) {
+      b.new_L[rd.shell_off + c] = logL0;
+      b.new_E[rd.shell_off + c] = total;
+      if (flags & LG_FAILED) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
+      atomicSub(&lg.chains_left[r], 1);
+    }
   } else {
     if (flags & LG_NEED_DIR) {
       if (P == 1) {
-        d[0] = 1.0f;
+        da = 1.0;
       } else {
-        float ssd = 0.0f;
-        for (int p = 0; p < P; ++p) {
-          const float v = normal_from_bits(bits64(dir_key, (uint32_t)p));
-          d[p] = v;
-          ssd = fmaf(v, v, ssd);
-        }
-        const float nrm = sqrtf(ssd);
-        for (int p = 0; p < P; ++p) d[p] = d[p] / nrm;
+        const float va = ha ? normal_from_bits(bits64(dir_key, (uint32_t)pa_)) : 0.0f;
+        const float vb = hb ? normal_from_bits(bits64(dir_key, (uint32_t)pb_)) : 0.0f;
+        const double inv = 1.0 / sqrt((double)warp_sum(fmaf(va, va, vb * vb)));
+        da = (double)va * inv;
+        db = (double)vb * inv;
       }
+      d_changed = true;
       flags &= ~LG_NEED_DIR;
     }
     const bool start = (flags & LG_START) != 0;
@@ -169,58 +188,88 @@ __global__ void k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
     if (start) {
       after_key = fold(B, 3u);
       alpha = lg_alpha(j, S);
-      float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
-      for (int p = 0; p < P; ++p) {
-        const float t1 = (1.0f - u0[p]) / d[p], t0 = -u0[p] / d[p];
-        t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
-        t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
-        t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
-        t0l = fmaxf(t0l, t0 <= 0.f ? t0 : -INFINITY);
+      double t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const bool have = h ? hb : ha;
+        if (have) {
+          const double uu = h ? ub : ua, dd = h ? db : da;
+          const double t1 = (1.0 - uu) / dd, t0 = -uu / dd;
+          t1r = fmin(t1r, t1 >= 0.0 ? t1 : INFINITY);
+          t1l = fmax(t1l, t1 <= 0.0 ? t1 : -INFINITY);
+          t0r = fmin(t0r, t0 >= 0.0 ? t0 : INFINITY);
+          t0l = fmax(t0l, t0 <= 0.0 ? t0 : -INFINITY);
+        }
       }
-      right = fminf(t0r, t1r);
-      left = fmaxf(t0l, t1l);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        t1r = fmin(t1r, __shfl_xor_sync(0xffffffffu, t1r, o));
+        t1l = fmax(t1l, __shfl_xor_sync(0xffffffffu, t1l, o));
+        t0r = fmin(t0r, __shfl_xor_sync(0xffffffffu, t0r, o));
+        t0l = fmax(t0l, __shfl_xor_sync(0xffffffffu, t0l, o));
+      }
+      right = fmin(t0r, t1r);
+      left = fmax(t0l, t1l);
       in_slice = 0;
     } else {
-      if (t < 0.f) left = t;
-      if (t > 0.f) right = t;
+      if (t < 0.0) left = t;
+      if (t > 0.0) right = t;
       if (rd.midpoint) {
-        if (t < 0.f) left = alpha * left;
-        if (t > 0.f) right = alpha * right;
+        if (t < 0.0) left = __dmul_rn(alpha, left);
+        if (t > 0.0) right = __dmul_rn(alpha, right);
       }
     }
-    t = fmaf(uniform01(bits64(tk, 0u)), right - left, left);
+    // _pick_point_in_interval (uni_slice_sampler.py:67-89): t = left + u (right - left)
+    t = __dadd_rn(left, __dmul_rn(uniform01_d(bits64(tk, 0u)), __dsub_rn(right, left)));
     const int *kind = b.prior_kind + rd.prior_off;
     const float *pa = b.prior_a + rd.prior_off, *pb = b.prior_b + rd.prior_off;
+    const float wa = ha ? prior_quantile_d(kind[pa_], pa[pa_], pb[pa_], __dadd_rn(ua, __dmul_rn(t, da))) : 0.0f;
+    const float wb = hb ? prior_quantile_d(kind[pb_], pa[pb_], pb[pb_], __dadd_rn(ub, __dmul_rn(t, db))) : 0.0f;
     if (lg.use_tc) {
       float *wh = lg.W_hi + (size_t)g * 64, *wl = lg.W_lo + (size_t)g * 64;
-      for (int p = 0; p < P; ++p) tf32_split(prior_quantile(kind[p], pa[p], pb[p], fmaf(t, d[p], u0[p])), wh[p], wl[p]);
+      if (ha) tf32_split(wa, wh[pa_], wl[pa_]);
+      if (hb) tf32_split(wb, wh[pb_], wl[pb_]);
     } else {
-      for (int p = 0; p < P; ++p) W[p] = prior_quantile(kind[p], pa[p], pb[p], fmaf(t, d[p], u0[p]));
+      float *W = lg.W + du + (size_t)c * P;
+      if (ha) W[pa_] = wa;
+      if (hb) W[pb_] = wb;
     }
     flags |= LG_PENDING;
   }
-  lg.flags[g] = flags;
-  lg.j[g] = j;
-  lg.total[g] = total;
-  lg.in_slice[g] = in_slice;
-  lg.left[g] = left;
-  lg.right[g] = right;
-  lg.t[g] = t;
-  lg.alpha[g] = alpha;
-  lg.logL0[g] = logL0;
-  lg.ck[2 * g] = ck.k0;
-  lg.ck[2 * g + 1] = ck.k1;
-  lg.after_key[2 * g] = after_key.k0;
-  lg.after_key[2 * g + 1] = after_key.k1;
-  lg.dir_key[2 * g] = dir_key.k0;
-  lg.dir_key[2 * g + 1] = dir_key.k1;
+  if (u_changed) {
+    if (ha) u0[pa_] = ua;
+    if (hb) u0[pb_] = ub;
+  }
+  if (d_changed) {
+    if (ha) d[pa_] = da;
+    if (hb) d[pb_] = db;
+  }
+  if (lane == 0) {
+    lg.ss[g] = 0.0;
+    lg.flags[g] = flags;
+    lg.j[g] = j;
+    lg.total[g] = total;
+    lg.in_slice[g] = in_slice;
+    lg.left[g] = left;
+    lg.right[g] = right;
+    lg.t[g] = t;
+    lg.alpha[g] = alpha;
+    lg.logL0[g] = logL0;
+    lg.ck[2 * g] = ck.k0;
+    lg.ck[2 * g + 1] = ck.k1;
+    lg.after_key[2 * g] = after_key.k0;
+    lg.after_key[2 * g + 1] = after_key.k1;
+    lg.dir_key[2 * g] = dir_key.k0;
+    lg.dir_key[2 * g + 1] = dir_key.k1;
+  }
 }
 
 // |y - Phi w|^2 (and y . (y - Phi w)) for a 64-point x 64-row tile; FP64 atomics per point.
-// Points are rows of W (the pending proposals, or the dead set for the adjoint); in adjoint
-// mode W comes from U: w = tau * ndtri(u).
+// Points are rows of W (the pending proposals), or for the adjoint rows of an FP64 U with
+// w = tau * ndtri(u).
 template <int PMAX>
-__device__ __forceinline__ void resid_tile(const float *__restrict__ Wsrc, bool from_U, float tau, int npts, int P,
+__device__ __forceinline__ void resid_tile(const float *__restrict__ Wsrc, const double *__restrict__ Usrc, float tau,
+                                           int npts, int P,
                                            const float *__restrict__ Phi, const float *__restrict__ y, int N,
                                            int row0, double *ss_out, double *ry_out) {
   __shared__ float Ws[64][PMAX + 1];
@@ -233,8 +282,7 @@ __device__ __forceinline__ void resid_tile(const float *__restrict__ Wsrc, bool 
     const int i = q / PMAX, k = q % PMAX;
     float w = 0.0f;
     if (i < npts && k < P) {
-      const float v = Wsrc[(size_t)i * P + k];
-      w = from_U ? tau * (GBNS_SQRT2F * erfinvf(fmaf(2.0f, v, -1.0f))) : v;
+      w = Usrc ? tau * ndtri_from_double(Usrc[(size_t)i * P + k]) : Wsrc[(size_t)i * P + k];
     }
     Ws[i][k] = w;
     const int row = row0 + i;
@@ -298,19 +346,22 @@ __global__ void __launch_bounds__(256) k_lg_resid(gbns_batch b, gbns_lg_bufs lg)
   const gbns_run_desc &rd = b.runs[r];
   const gbns_run_state &st = b.state[r];
   if (st.done || st.phase != 1) return;
+  const int t = threadIdx.x;
+  const bool pending = t < nc && (lg.flags[rd.shell_off + c0 + t] & LG_PENDING) != 0;
+  if (!__syncthreads_or(pending)) return;
   const int P = rd.D, N = rd.N;
   const float *fp = b.fparams + rd.param_off;
-  resid_tile<PMAX>(lg.W + rd.newU_off + (size_t)c0 * P, false, 0.0f, nc, P, fp, fp + (size_t)N * P, N, row0,
+  resid_tile<PMAX>(lg.W + (rd.newU_off >> 1) + (size_t)c0 * P, nullptr, 0.0f, nc, P, fp, fp + (size_t)N * P, N, row0,
                    lg.ss + rd.shell_off + c0, nullptr);
 }
 
 template <int PMAX>
-__global__ void __launch_bounds__(256) k_adj_resid(const float *U, long long M, int P, const float *Phi, const float *y,
+__global__ void __launch_bounds__(256) k_adj_resid(const double *U, long long M, int P, const float *Phi, const float *y,
                                                    int N, float tau, double *ss, double *ry) {
   const long long p0 = (long long)blockIdx.x * 64;
   const int row0 = blockIdx.y * 64;
   const int npts = (int)min(64ll, M - p0);
-  resid_tile<PMAX>(U + p0 * P, true, tau, npts, P, Phi, y, N, row0, ss + p0, ry + p0);
+  resid_tile<PMAX>(nullptr, U + p0 * P, tau, npts, P, Phi, y, N, row0, ss + p0, ry + p0);
 }
 
 // log Z(theta) = logsumexp_i a_i, a_i = log L_theta(U_i) + log w_i, and its gradient
@@ -356,25 +407,30 @@ cudaError_t launch_lg_begin(const gbns_batch &b, const gbns_lg_bufs &lg, long lo
 }
 
 cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
-  if (lg.total_chains > 0)
-    k_lg_step<<<(unsigned)((lg.total_chains + 127) / 128), 128, 0, s>>>(b, lg, lg.total_chains);
+  if (lg.total_chains > 0)  // 8 chains (warps) per CTA
+    k_lg_step<<<(unsigned)((lg.total_chains + 7) / 8), 256, 0, s>>>(b, lg, lg.total_chains);
   return cudaGetLastError();
 }
 
-cudaError_t launch_lg_steps(const gbns_batch &b, const gbns_lg_bufs &lg, long long total_chains, int pmax, int steps,
-                            cudaStream_t s) {
-  if (lg.use_tc) return launch_lg_steps_tc(b, lg, steps, s);
-  for (int q = 0; q < steps; ++q) {
-    k_lg_step<<<(unsigned)((total_chains + 127) / 128), 128, 0, s>>>(b, lg, total_chains);
-    if (lg.num_items > 0) {
-      if (pmax <= 32) k_lg_resid<32><<<lg.num_items, 256, 0, s>>>(b, lg);
-      else k_lg_resid<64><<<lg.num_items, 256, 0, s>>>(b, lg);
-    }
+cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
+  if (lg.num_items > 0) {
+    if (lg.pmax <= 32) k_lg_resid<32><<<lg.num_items, 256, 0, s>>>(b, lg);
+    else k_lg_resid<64><<<lg.num_items, 256, 0, s>>>(b, lg);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint(const float *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
+cudaError_t launch_lg_steps(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t s) {
+  if (lg.use_tc) return launch_lg_steps_tc(b, lg, steps, s);
+  for (int q = 0; q < steps; ++q) {
+    cudaError_t e = launch_lg_step_kernel(b, lg, s);
+    if (e == cudaSuccess) e = launch_lg_resid_cc(b, lg, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const double *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
                            int N, double log_tau, double log_sigma, double *out, double *ss, double *ry,
                            cudaStream_t s) {
   cudaError_t e = cudaMemsetAsync(ss, 0, sizeof(double) * M, s);
@@ -428,12 +484,30 @@ int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps
   int rc = lg_check(batch, lg);
   if (rc) return rc;
   if (num_steps < 0) return lg_fail(-1, "gbns_lg_steps: negative step count");
-  cudaError_t e = gbns::launch_lg_steps(*batch, *lg, lg->total_chains, lg->pmax, num_steps, (cudaStream_t)stream);
+  cudaError_t e = gbns::launch_lg_steps(*batch, *lg, num_steps, (cudaStream_t)stream);
   if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
   return 0;
 }
 
-int gbns_evidence_adjoint(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+// The two halves of one step, for callers that interleave their own work (e.g. timing events).
+int gbns_lg_chain_step(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
+  int rc = lg_check(batch, lg);
+  if (rc) return rc;
+  cudaError_t e = gbns::launch_lg_step_kernel(*batch, *lg, (cudaStream_t)stream);
+  if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+int gbns_lg_residual(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
+  int rc = lg_check(batch, lg);
+  if (rc) return rc;
+  cudaError_t e = lg->use_tc ? gbns::launch_lg_steps_tc(*batch, *lg, -1, (cudaStream_t)stream)
+                             : gbns::launch_lg_resid_cc(*batch, *lg, (cudaStream_t)stream);
+  if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+int gbns_evidence_adjoint(const double *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
                           const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
                           double *ss_scratch_dev, double *ry_scratch_dev, void *stream) {
   if (M < 0 || P < 1 || P > 64 || N < 1 || !out_dev || (M > 0 && (!U_dev || !log_w_dev || !ss_scratch_dev ||

@@ -236,6 +236,11 @@ __global__ void __launch_bounds__(128) k_lg_resid_tc(const __grid_constant__ TcM
   const gbns_run_desc &rd = b.runs[r];
   gbns_run_state &st = b.state[r];
   if (st.done || st.phase != 1) return;
+  // skip the tile when none of its chains has a pending proposal (finished chains keep
+  // stepping in lock step with the slowest chain of the batch)
+  const int t = threadIdx.x;
+  const bool pending = t < nc && (lg.flags[rd.shell_off + c0 + t] & LG_PENDING) != 0;
+  if (!__syncthreads_or(pending)) return;
   const int P = rd.D, N = rd.N;
   const float *y = b.fparams + rd.param_off + (size_t)N * P;
   tc_resid_tile(maps, (int)(rd.shell_off + c0), (int)(lg.row_base[r] + row0), (P + TC_KB - 1) / TC_KB, (P + 7) / 8,
@@ -272,7 +277,7 @@ __global__ void k_split_phi(gbns_batch b, gbns_lg_bufs lg) {
 
 // Dead points for the adjoint: w = tau * sqrt(2) * erfinv(2u - 1) (the Normal(0, tau^2)
 // quantile), and Phi, both as TF32 hi/lo rows of ld floats.
-__global__ void k_adj_split(const float *U, long long M, int P, const float *Phi, int N, float tau, int ld,
+__global__ void k_adj_split(const double *U, long long M, int P, const float *Phi, int N, float tau, int ld,
                             float *w_hi, float *w_lo, float *phi_hi, float *phi_lo) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long nw = M * ld, np = (long long)N * ld;
@@ -281,7 +286,7 @@ __global__ void k_adj_split(const float *U, long long M, int P, const float *Phi
   if (q < nw) {
     const long long i = q / ld;
     const int k = (int)(q % ld);
-    if (k < P) tf32_split(tau * (GBNS_SQRT2F * erfinvf(fmaf(2.0f, U[i * P + k], -1.0f))), h, l);
+    if (k < P) tf32_split(tau * ndtri_from_double(U[i * P + k]), h, l);
     w_hi[q] = h;
     w_lo[q] = l;
   } else {
@@ -356,7 +361,7 @@ cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStrea
 }
 
 // steps x (chain step + tensor-core residual over lg.items_tc); the TMA descriptors are
-// encoded once per call from lg's buffers.
+// encoded once per call from lg's buffers.  steps = -1: one residual launch, no chain step.
 cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t s) {
   cudaError_t e = set_smem_attrs();
   if (e != cudaSuccess) return e;
@@ -367,6 +372,10 @@ cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int 
       !encode_rows(&maps.b_lo, lg.Phi_lo, lg.total_rows, 64, TC_N))
     return cudaErrorInvalidValue;
   const int nkb = lg.pmax > TC_KB ? 2 : 1;
+  if (steps < 0) {
+    if (lg.num_items_tc > 0) k_lg_resid_tc<<<lg.num_items_tc, 128, nkb * TC_KB_BYTES + 1024, s>>>(maps, b, lg);
+    return cudaGetLastError();
+  }
   for (int q = 0; q < steps; ++q) {
     e = launch_lg_step_kernel(b, lg, s);
     if (e != cudaSuccess) return e;
@@ -375,7 +384,7 @@ cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int 
   return cudaGetLastError();
 }
 
-cudaError_t launch_adjoint_tc(const float *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
+cudaError_t launch_adjoint_tc(const double *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
                               int N, double log_tau, double log_sigma, double *out, double *ss, double *ry,
                               float *w_scratch, float *phi_scratch, int *status, cudaStream_t s) {
   cudaError_t e = set_smem_attrs();
@@ -418,7 +427,7 @@ int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *st
   return 0;
 }
 
-int gbns_evidence_adjoint_tc(const float *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
+int gbns_evidence_adjoint_tc(const double *U_dev, const double *log_w_dev, long long M, int P, const float *Phi_dev,
                              const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
                              double *ss_scratch_dev, double *ry_scratch_dev, float *w_scratch_dev,
                              float *phi_scratch_dev, int *status_dev, void *stream) {

@@ -160,7 +160,7 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
   const gbns_run_state &st = b.state[r];
   const long long N = st.num_samples < rd.cap ? st.num_samples : rd.cap;
   const long long so = rd.store_off;
-  const int D = rd.D;
+  const int D = rd.ucols;  // 32-bit words of U per sample
   unsigned long long *scratch = (unsigned long long *)res.scratch_ll + 2 * (so + r);
   int *deg = res.scratch_i + (so + r);
   int *si = res.samples_indices + so;

@@ -126,6 +126,9 @@ class NSBatch:
         self.R = R
         dev = self.device
         Ds = np.array([s.D for s in specs])
+        # 32-bit words of U storage per point: the linear-Gaussian family keeps U in FP64
+        Ws = np.array([2 * s.D if s.family == FAMILY_LINGAUSS else s.D for s in specs])
+        self.ucols = Ws
         ns = np.array([s.num_live_points for s in specs])
         ss = np.array([s.shell_size for s in specs])
         Ks = np.array([s.num_phantom for s in specs])
@@ -145,13 +148,13 @@ class NSBatch:
         param_off = np.concatenate([[0], np.cumsum(plen)[:-1]])
         prior_off = np.concatenate([[0], np.cumsum(Ds)[:-1]])
         ustore = np.array([s.store_U for s in specs])
-        ucap = np.where(ustore, caps * Ds, 0)
+        ucap = np.where(ustore, caps * Ws, 0)
         ustore_off = np.where(ustore, np.concatenate([[0], np.cumsum(ucap)[:-1]]), -1)
         excl = lambda v: np.concatenate([[0], np.cumsum(v)[:-1]]).astype(np.int64)
-        liveU_off, newU_off = excl(ns * Ds), excl(ss * Ds)
-        phU_off, phL_off = excl(ss * Ks * Ds), excl(ss * Ks)
+        liveU_off, newU_off = excl(ns * Ws), excl(ss * Ws)
+        phU_off, phL_off = excl(ss * Ks * Ws), excl(ss * Ks)
         self.offsets = dict(live=live_off, store=store_off, shell=shell_off, ustore=ustore_off, liveU=liveU_off,
-                            newU=newU_off)
+                            newU=newU_off, param=param_off)
 
         descs = (_ffi.RunDesc * R)()
         for r, s in enumerate(specs):
@@ -160,6 +163,7 @@ class NSBatch:
             d.family, d.midpoint = s.family, int(bool(s.midpoint_shrink))
             d.uniform_phase = int(s.init_efficiency_threshold > 0.0)
             d.N = s.N
+            d.ucols = int(Ws[r])
             d.init_efficiency_threshold = float(s.init_efficiency_threshold)
             d.log_L_offset = float(s.log_L_offset)
             d.cap = int(caps[r])
@@ -180,7 +184,7 @@ class NSBatch:
         self._state_host0 = u8(st).pin_memory() if torch.cuda.is_available() else u8(st)
 
         nsum, ssum, capsum = int(ns.sum()), int(ss.sum()), int(caps.sum())
-        nD = int((ns * Ds).sum())
+        nD = int((ns * Ws).sum())
         f32, i32 = torch.float32, torch.int32
         z = lambda *shape, dtype=f32: torch.zeros(*shape, dtype=dtype, device=dev)
         self.live_U = [z(nD), z(nD)]
@@ -188,10 +192,10 @@ class NSBatch:
         self.live_Lc = [z(nsum), z(nsum)]
         self.live_E = [z(nsum, dtype=i32), z(nsum, dtype=i32)]
         self.live_S = [z(nsum, dtype=i32), z(nsum, dtype=i32)]
-        self.new_U = z(int((ss * Ds).sum()))
+        self.new_U = z(int((ss * Ws).sum()))
         self.new_L = z(ssum)
         self.new_E = z(ssum, dtype=i32)
-        self.ph_U = z(max(int((ss * Ks * Ds).sum()), 1))
+        self.ph_U = z(max(int((ss * Ks * Ws).sum()), 1))
         self.ph_L = z(max(int((ss * Ks).sum()), 1))
         self.store_L = torch.full((capsum,), float("inf"), dtype=f32, device=dev)
         self.store_S = z(capsum, dtype=i32)
@@ -199,7 +203,9 @@ class NSBatch:
         self.store_P = z(capsum, dtype=torch.uint8)
         usum = int(ucap.sum())
         self.store_U = z(usum) if usum > 0 else None
-        self.fparams = torch.from_numpy(np.concatenate([np.asarray(s.params, np.float32) for s in specs])).to(dev)
+        fp_host = torch.from_numpy(np.concatenate([np.asarray(s.params, np.float32) for s in specs]))
+        self._fparams_host = fp_host.pin_memory() if torch.cuda.is_available() else fp_host
+        self.fparams = fp_host.to(dev)
         self.prior_kind = torch.from_numpy(np.concatenate([np.asarray(s.prior_kind, np.int32) for s in specs])).to(dev)
         self.prior_a = torch.from_numpy(np.concatenate([np.asarray(s.prior_a, np.float32) for s in specs])).to(dev)
         self.prior_b = torch.from_numpy(np.concatenate([np.asarray(s.prior_b, np.float32) for s in specs])).to(dev)
@@ -259,6 +265,8 @@ class NSBatch:
         self.timing = False
         self.shell_ms = 0.0
         self.shell_launch_groups = 0
+        self.resid_ms = 0.0
+        self.resid_launches = 0
         self.iterations_run = 0
         self.kernel_launches = 0
         self._kernels_per_iter = 1 + int(np.count_nonzero(be > bb))
@@ -271,11 +279,12 @@ class NSBatch:
         nc = int(ss.sum())
         nd = int((ss * Ds).sum())
         z = lambda n, dt=torch.float32: torch.zeros(max(n, 1), dtype=dt, device=dev)
+        f64 = torch.float64
         self.lg_t = dict(j=z(nc, torch.int32), in_slice=z(nc, torch.int32), total=z(nc, torch.int32),
-                         flags=z(nc, torch.int32), left=z(nc), right=z(nc), t=z(nc), alpha=z(nc), logL0=z(nc),
-                         ck=z(2 * nc, torch.int32), after_key=z(2 * nc, torch.int32),
-                         slices_key=z(2 * nc, torch.int32), dir_key=z(2 * nc, torch.int32), u0=z(nd), dir=z(nd),
-                         W=z(nd), ss=z(nc, torch.float64), chains_left=z(len(specs), torch.int32))
+                         flags=z(nc, torch.int32), left=z(nc, f64), right=z(nc, f64), t=z(nc, f64),
+                         alpha=z(nc, f64), logL0=z(nc), ck=z(2 * nc, torch.int32), after_key=z(2 * nc, torch.int32),
+                         slices_key=z(2 * nc, torch.int32), dir_key=z(2 * nc, torch.int32), u0=z(nd, f64),
+                         dir=z(nd, f64), W=z(nd), ss=z(nc, f64), chains_left=z(len(specs), torch.int32))
         items = []
         for r, s in enumerate(specs):
             for c0 in range(0, s.shell_size, 64):
@@ -331,17 +340,33 @@ class NSBatch:
         self.kernel_launches += k * self._kernels_per_iter
 
     def _lg_graph(self, k: int):
-        ent = self._graphs.get(("lg", k))
+        """CUDA graph of k lock-step steps; when timing, each residual launch is bracketed by
+        events recorded by the graph itself."""
+        key = ("lg", k, self.timing)
+        ent = self._graphs.get(key)
         if ent is None:
             g = torch.cuda.CUDAGraph()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(k)] if self.timing else []
+            for a, b_ in evs:
+                a.record()
+                b_.record()
+            torch.cuda.current_stream().synchronize()
             side = torch.cuda.Stream(device=self.device)
             side.wait_stream(torch.cuda.current_stream())
             with torch.cuda.graph(g, stream=side):
-                _ffi.call("gbns_lg_steps", ctypes.byref(self._b), ctypes.byref(self._lgb), int(k), self._stream())
+                if self.timing:
+                    for a, b_ in evs:
+                        _ffi.call("gbns_lg_chain_step", ctypes.byref(self._b), ctypes.byref(self._lgb), self._stream())
+                        _ffi.call("gbns_record_event", ctypes.c_void_p(a.cuda_event), self._stream())
+                        _ffi.call("gbns_lg_residual", ctypes.byref(self._b), ctypes.byref(self._lgb), self._stream())
+                        _ffi.call("gbns_record_event", ctypes.c_void_p(b_.cuda_event), self._stream())
+                else:
+                    _ffi.call("gbns_lg_steps", ctypes.byref(self._b), ctypes.byref(self._lgb), int(k), self._stream())
             torch.cuda.current_stream().wait_stream(side)
-            ent = (g, [])
-            self._graphs[("lg", k)] = ent
-        return ent[0]
+            ent = (g, evs)
+            self._graphs[key] = ent
+        return ent
 
     def _lg_iteration(self, use_graph: bool = True, block: int = 64):
         """One NS iteration of the linear-Gaussian batch: start the shell, advance every chain
@@ -355,13 +380,18 @@ class NSBatch:
         cap = int(max(s.num_slices for s in self.specs)) * 2000
         steps = 0
         while True:
+            evs = []
             if use_graph:
-                self._lg_graph(block).replay()
+                g, evs = self._lg_graph(block)
+                g.replay()
             else:
                 _ffi.call("gbns_lg_steps", ctypes.byref(self._b), ctypes.byref(self._lgb), int(block), self._stream())
             steps += block
             self.kernel_launches += 2 * block
             left = self.lg_t["chains_left"].cpu().numpy()
+            if evs:
+                self.resid_ms += sum(a.elapsed_time(b_) for a, b_ in evs)
+                self.resid_launches += len(evs)
             if not np.any(left[active] > 0):
                 break
             if steps > cap:
@@ -414,6 +444,15 @@ class NSBatch:
             self.shell_ms += sum(a.elapsed_time(b_) for a, b_ in evs)
             self.shell_launch_groups += len(evs)
         self._pending_events = None
+
+    def upload_params(self):
+        """Copy the likelihood parameters (MVN factors, shell centres, Phi and y) from pinned
+        host memory to the device again, and re-split Phi for the tensor-core path."""
+        self.fparams.copy_(self._fparams_host, non_blocking=True)
+        if self.lg and self.lg_tc:
+            _ffi.call("gbns_lg_prepare_tc", ctypes.byref(self._b), ctypes.byref(self._lgb), self._stream())
+            self.kernel_launches += 1
+        return int(self.fparams.numel() * 4)
 
     def reset(self, from_host: bool = False):
         """Restore every run's initial state (keys); from_host copies it from pinned memory."""
@@ -504,7 +543,7 @@ class NSBatch:
         d = {k: v[o:o + N] for k, v in out.items() if k not in ("scalars", "U_sorted") and v is not None}
         if out.get("U_sorted") is not None and self.offsets["ustore"][r] >= 0:
             uo = int(self.offsets["ustore"][r])
-            d["U_sorted"] = out["U_sorted"][uo:uo + N * s.D].view(N, s.D)
+            d["U_sorted"] = self._u_rows(out["U_sorted"][uo:uo + N * int(self.ucols[r])], r, N)
         d["scalars"] = out["scalars"][r]
         return d
 
@@ -518,8 +557,21 @@ class NSBatch:
                  nevals=self.store_E[o:o + N], phantom=self.store_P[o:o + N])
         if self.store_U is not None and self.offsets["ustore"][r] >= 0:
             uo = int(self.offsets["ustore"][r])
-            d["U"] = self.store_U[uo:uo + N * s.D].view(N, s.D)
+            d["U"] = self._u_rows(self.store_U[uo:uo + N * int(self.ucols[r])], r, N)
         return d
+
+    def _u_rows(self, words: torch.Tensor, r: int, rows: int) -> torch.Tensor:
+        """[rows, D] view of run r's U words (float64 for the linear-Gaussian family)."""
+        D = self.specs[r].D
+        if self.specs[r].family == FAMILY_LINGAUSS:
+            return words.view(torch.float64).view(rows, D)
+        return words.view(rows, D)
+
+    def new_U_view(self, r: int) -> torch.Tensor:
+        """[s, D] view of run r's shell outputs (the chains' final points)."""
+        o = int(self.offsets["newU"][r])
+        s = self.specs[r].shell_size
+        return self._u_rows(self.new_U[o:o + s * int(self.ucols[r])], r, s)
 
     def live_view(self, r: int) -> Dict[str, torch.Tensor]:
         st = self.state()
@@ -529,13 +581,16 @@ class NSBatch:
         uo = int(self.offsets["liveU"][r])
         n = s.num_live_points
         raw = self.live_L[p][o:o + n]
-        return dict(U=self.live_U[p][uo:uo + n * s.D].view(n, s.D), log_L=raw.double() + s.log_L_offset, log_L_raw=raw,
+        return dict(U=self._u_rows(self.live_U[p][uo:uo + n * int(self.ucols[r])], r, n),
+                    log_L=raw.double() + s.log_L_offset, log_L_raw=raw,
                     nevals=self.live_E[p][o:o + n], sender=self.live_S[p][o:o + n],
                     log_L_constraint=self.live_Lc[p][o:o + n])
 
     def forward(self, r: int, U: torch.Tensor) -> torch.Tensor:
-        """Model.forward of run r over a batch U [B, D] (device tensor)."""
-        U = U.to(device=self.device, dtype=torch.float32).contiguous()
+        """Model.forward of run r over a batch U [B, D] (device tensor; FP64 for the
+        linear-Gaussian family)."""
+        dt = torch.float64 if self.specs[r].family == FAMILY_LINGAUSS else torch.float32
+        U = U.to(device=self.device, dtype=dt).contiguous()
         out = torch.empty(U.shape[0], dtype=torch.float32, device=self.device)
         _ffi.call("gbns_forward", ctypes.byref(self._b), int(r), ctypes.c_void_p(U.data_ptr()),
                   ctypes.c_void_p(out.data_ptr()), ctypes.c_longlong(U.shape[0]), self._stream())
@@ -559,7 +614,9 @@ class NSBatch:
         o = int(self.offsets["live"][r])
         uo = int(self.offsets["liveU"][r])
         n = s.num_live_points
-        self.live_U[p][uo:uo + n * s.D].copy_(torch.from_numpy(np.asarray(U, np.float32).ravel()))
+        dt = np.float64 if s.family == FAMILY_LINGAUSS else np.float32
+        words = torch.from_numpy(np.ascontiguousarray(np.asarray(U, dt).ravel()).view(np.float32))
+        self.live_U[p][uo:uo + n * int(self.ucols[r])].copy_(words)
         self.live_L[p][o:o + n].copy_(torch.from_numpy(np.asarray(log_L, np.float32)))
 
 
