@@ -219,6 +219,10 @@ def main():
                     help="config3: keep only runs of this dimension (repeated to --runs); for kernel profiling")
     ap.add_argument("--plain-problems", type=int, default=4,
                     help="blr workloads: problems in the plain GPU + finite-difference comparison")
+    ap.add_argument("--kernel-profile", action="store_true",
+                    help="blr workloads: init + --iterations NS iterations only (for ncu)")
+    ap.add_argument("--cuda-core", action="store_true",
+                    help="blr workloads: fp32 CUDA-core residuals instead of the tcgen05 kernel")
     ap.add_argument("--iterations", type=int, default=None,
                     help="time init + this many NS iterations instead of whole runs (kernel profiling)")
     args = ap.parse_args()
@@ -527,8 +531,23 @@ def main_blr(args):
     wl = blr_workload(args.runs, 2024 + rank, name)
     R = len(wl)
     keys = np.array([gb.random.PRNGKey(r) for r in range(R)])
-    bns = BatchedNestedSampler([blr_sampler(p) for p in wl], keys, None, store_U=True)
+    bns = BatchedNestedSampler([blr_sampler(p) for p in wl], keys, None, store_U=not args.kernel_profile,
+                               lg_tensor_cores=not args.cuda_core)
     b = bns.batch
+    if args.kernel_profile:
+        # kernel-profiling mode: init + a fixed number of NS iterations (eager launches)
+        T = args.iterations or 2
+        b.init()
+        torch.cuda.synchronize()
+        t0 = time.time()
+        for _ in range(T):
+            b._lg_iteration(use_graph=False)
+        torch.cuda.synchronize()
+        st = b.state()
+        print(json.dumps({"mode": "kernel-profile", "iterations": T, "problems": R, "seconds": time.time() - t0,
+                          "lock_step_steps": b.lg_steps_run,
+                          "likelihood_evals": int(st["num_likelihood_evaluations"].sum())}))
+        return
     thetas = np.array([[np.log(p["tau"]), np.log(p["sigma"])] for p in wl])
 
     def barrier():

@@ -179,10 +179,10 @@ typedef struct {
  * indexed like the shell outputs ([sum s] and [sum s * D]). */
 typedef struct {
     int *j, *in_slice, *total, *flags;      /* [sum s] */
-    double *left, *right, *t, *alpha;       /* [sum s] slice interval, point, shrink factor (U space, FP64) */
-    float *logL0;                           /* [sum s] */
+    float *left, *right, *t, *alpha, *logL0; /* [sum s] slice interval, point, shrink factor */
     uint32_t *ck, *after_key, *slices_key, *dir_key; /* [sum s * 2] */
-    double *u0, *dir;                       /* [sum s * D]: seed point and direction (U space, FP64) */
+    float *u0, *u0_lo, *dir;                /* [sum s * D]: seed point as an fp32 pair u0 + u0_lo (U space
+                                               to ~1e-14 near 0 and 1), direction */
     float *W;                               /* [sum s * D]: proposal w (CUDA-core residual path) */
     double *ss;                             /* [sum s] residual sums of the pending proposals */
     int *chains_left;                       /* [R] chains of the current shell not yet finished */
@@ -192,15 +192,25 @@ typedef struct {
     long long total_chains;                 /* sum of s over the runs */
     /* Tensor-core (tcgen05) residual path, used when use_tc != 0 (after gbns_lg_prepare_tc
      * has filled Phi_hi / Phi_lo).  Proposals and Phi are held as TF32 hi + lo parts, rows
-     * padded to 64 floats (256 B, zero beyond P); the contraction is hi*hi + hi*lo + lo*hi. */
+     * padded to 64 floats (256 B, zero beyond P); the contraction is hi*hi + hi*lo + lo*hi
+     * (3xTF32).  Work units: (run, 128-chain tile, range of 128-row tiles), walked by a
+     * persistent kernel of num_ctas_tc CTAs. */
     int use_tc;
     int num_items_tc;
-    const int *items_tc;                    /* [num_items_tc * 4]: (run, first chain, count <= 128, first row);
-                                               first chain a multiple of 128, first row a multiple of 256 */
+    const int *items_tc;                    /* [num_items_tc * 4]: (run, first chain (multiple of 128),
+                                               first 128-row tile, number of row tiles) */
     float *W_hi, *W_lo;                     /* [total_chains * 64], row = global chain index */
     float *Phi_hi, *Phi_lo;                 /* [total_rows * 64] */
     const long long *row_base;              /* [R] first row of each run in Phi_hi / Phi_lo */
     long long total_rows;                   /* sum of N over the runs */
+    int num_ctas_tc;                        /* cap on the persistent grid; 0 = one CTA per SM (two when
+                                               every P <= 32) */
+    int num_tiles;                          /* 128-chain tiles over all runs */
+    const int *chain_run;                   /* [total_chains] run of each chain */
+    const int *tile_base;                   /* [R] first 128-chain tile of each run */
+    int *tile_pending;                      /* [num_tiles] set by the chain step when a chain of the tile
+                                               has a pending proposal; cleared by the residual launch */
+    int *tc_done;                           /* [1] CTA completion counter of the residual launch (zeroed) */
 } gbns_lg_bufs;
 
 /* results buffers (device) */
@@ -283,7 +293,8 @@ int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps
 int gbns_lg_chain_step(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 int gbns_lg_residual(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 /* Split each run's Phi (fparams) into the TF32 hi/lo row-padded copies lg->Phi_hi / Phi_lo
- * used by the tensor-core residual path.  Call once per batch, before the first step. */
+ * read by the tensor-core residual path.  Call once per batch, before the first step (and
+ * after new parameters). */
 int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 
 /* Reweighted fixed-dead-point evidence of the linear-Gaussian model and its gradient

@@ -67,11 +67,12 @@ class LGBufs(ctypes.Structure):
     _fields_ = [("j", c_void_p), ("in_slice", c_void_p), ("total", c_void_p), ("flags", c_void_p),
                 ("left", c_void_p), ("right", c_void_p), ("t", c_void_p), ("alpha", c_void_p), ("logL0", c_void_p),
                 ("ck", c_void_p), ("after_key", c_void_p), ("slices_key", c_void_p), ("dir_key", c_void_p),
-                ("u0", c_void_p), ("dir", c_void_p), ("W", c_void_p), ("ss", c_void_p), ("chains_left", c_void_p),
+                ("u0", c_void_p), ("u0_lo", c_void_p), ("dir", c_void_p), ("W", c_void_p), ("ss", c_void_p), ("chains_left", c_void_p),
                 ("items", c_void_p), ("num_items", c_int), ("pmax", c_int), ("total_chains", c_ll),
                 ("use_tc", c_int), ("num_items_tc", c_int), ("items_tc", c_void_p), ("W_hi", c_void_p),
-                ("W_lo", c_void_p), ("Phi_hi", c_void_p), ("Phi_lo", c_void_p), ("row_base", c_void_p),
-                ("total_rows", c_ll)]
+                ("W_lo", c_void_p), ("Phi_hi", c_void_p), ("Phi_lo", c_void_p),
+                ("row_base", c_void_p), ("total_rows", c_ll), ("num_ctas_tc", c_int), ("num_tiles", c_int),
+                ("chain_run", c_void_p), ("tile_base", c_void_p), ("tile_pending", c_void_p), ("tc_done", c_void_p)]
 
 
 class ResultsBufs(ctypes.Structure):

@@ -8,17 +8,44 @@
 // residual kernel evaluates |y - Phi w|^2 for all proposals of the step at once.
 //
 // U is FP64 in this family (as in the reference, which runs in f64): with a Normal prior
-// the posterior can sit where u is within 1e-8 of 0 or 1, which fp32 cannot resolve.  The
-// slice arithmetic (seed, direction, bounds, point) is FP64; w = prior quantile is formed
-// in fp32 from an exactly computed tail argument (ndtri_from_double).  FP64 U is kept in
-// the float U buffers as pairs of 32-bit words (gbns_run_desc.ucols = 2 D), so the generic
-// merge / store / results kernels move it unchanged.  Chain-local offsets in doubles are
-// the float offsets halved.
+// the posterior can sit where u is within 1e-8 of 0 or 1, which fp32 cannot resolve.  FP64 U
+// is kept in the float U buffers as pairs of 32-bit words (gbns_run_desc.ucols = 2 D), so the
+// generic merge / store / results kernels move it unchanged.  Inside the lock-step kernels a
+// chain's point is an fp32 pair u = a + b (|b| <= ulp(a) / 2): FP64 runs at a small fraction
+// of the fp32 rate on this GPU, and the pair keeps what the tails need -- 1 - u = (1 - a) - b
+// is exact to fp32 relative precision, and a proposal adds its step t d into the low part.
+// FP64 is touched only when a chain loads its seed and stores its result.
 #include <cstdio>
 #include "gbns_device.cuh"
 #include "gbns_launch.h"
 
 namespace gbns {
+
+// fp32 pair <-> FP64
+__device__ __forceinline__ void pair_from_double(double u, float &a, float &b) {
+  a = (float)u;
+  b = (float)(u - (double)a);
+}
+
+// a + b as an fp32 pair (TwoSum: exact for any magnitudes).
+__device__ __forceinline__ void pair_add(float a, float s, float &hi, float &lo) {
+  hi = a + s;
+  const float bb = hi - a;
+  lo = (a - (hi - bb)) + (s - bb);
+}
+
+// Standard-normal quantile of u = a + s, in fp32 with the tail argument formed exactly.
+__device__ __forceinline__ float ndtri_pair(float a, float s) {
+  const float z = fmaf(2.0f, a, -1.0f) + 2.0f * s;  // 2u - 1 (2a - 1 exact for a in [1/4, 1])
+  if (fabsf(z) < 0.5f) return GBNS_SQRT2F * erfinvf(z);
+  if (a >= 0.5f) return GBNS_SQRT2F * erfcinvf(2.0f * ((1.0f - a) - s));
+  return -GBNS_SQRT2F * erfcinvf(2.0f * (a + s));
+}
+
+__device__ __forceinline__ float prior_quantile_pair(int kind, float pa, float pb, float a, float s) {
+  if (kind == GBNS_PRIOR_UNIFORM) return fmaf(pb, a, fmaf(pb, s, pa));
+  return fmaf(pb, ndtri_pair(a, s), pa);
+}
 
 __device__ __forceinline__ int run_of_chain(const gbns_batch &b, long long g) {
   int lo = 0, hi = b.num_runs;
@@ -29,12 +56,12 @@ __device__ __forceinline__ int run_of_chain(const gbns_batch &b, long long g) {
   return lo;
 }
 
-// linspace(0.5, 1, S)[j] (the midpoint shrink factors, uni_slice_sampler.py:114-273), FP64.
-__device__ __forceinline__ double lg_alpha(int j, int S) {
-  if (S == 1) return 0.5;
-  if (j == S - 1) return 1.0;
-  const double step = (double)j / (double)(S - 1);
-  return __dadd_rn(__dmul_rn(0.5, 1.0 - step), step);
+// linspace(0.5, 1, S)[j] (the midpoint shrink factors, uni_slice_sampler.py:114-273).
+__device__ __forceinline__ float lg_alpha(int j, int S) {
+  if (S == 1) return 0.5f;
+  if (j == S - 1) return 1.0f;
+  const float step = (float)j / (float)(S - 1);
+  return 0.5f * (1.0f - step) + step;
 }
 
 // A chain's first state of the shell: seed point (resample_indicies over log L > L*),
@@ -71,8 +98,8 @@ __global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
     if (lo64 & ((1ull << 52) - 1)) kk += 1;
     idx = (n - m) + (int)kk - 1;
   }
-  double *u0 = lg.u0 + (rd.newU_off >> 1) + (size_t)c * P;
-  for (int p = 0; p < P; ++p) u0[p] = liveU[(size_t)idx * P + p];
+  const size_t co = (rd.newU_off >> 1) + (size_t)c * P;
+  for (int p = 0; p < P; ++p) pair_from_double(liveU[(size_t)idx * P + p], lg.u0[co + p], lg.u0_lo[co + p]);
   lg.logL0[g] = liveL[idx];
   const Key dk = fold(chain_key, 0u), sk = fold(chain_key, 1u);
   lg.dir_key[2 * g] = dk.k0;
@@ -95,7 +122,7 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
   const long long g = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (g >= total_chains) return;
-  const int r = run_of_chain(b, g);
+  const int r = lg.chain_run ? lg.chain_run[g] : run_of_chain(b, g);
   const gbns_run_desc &rd = b.runs[r];
   gbns_run_state &st = b.state[r];
   if (rd.family != GBNS_LIK_LINGAUSS || st.done || st.phase != 1) return;
@@ -110,14 +137,14 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
   const float sigma = fp[(size_t)N * P + N];
   const float inv2s2 = 0.5f / (sigma * sigma);
   const float Lstar = b.live_L[st.parity][rd.live_off + rd.s - 1];
-  const long long du = rd.newU_off >> 1;  // chain vectors in doubles
-  double *u0 = lg.u0 + du + (size_t)c * P;
-  double *d = lg.dir + du + (size_t)c * P;
-  double ua = ha ? u0[pa_] : 0.0, ub = hb ? u0[pb_] : 0.0;
-  double da = ha ? d[pa_] : 0.0, db = hb ? d[pb_] : 0.0;
+  const long long du = rd.newU_off >> 1;  // chain vectors: D floats per chain
+  float *u0 = lg.u0 + du + (size_t)c * P, *u0l = lg.u0_lo + du + (size_t)c * P;
+  float *d = lg.dir + du + (size_t)c * P;
+  float ua = ha ? u0[pa_] : 0.0f, ub = hb ? u0[pb_] : 0.0f;      // seed point: (ua, la), (ub, lb)
+  float la = ha ? u0l[pa_] : 0.0f, lb = hb ? u0l[pb_] : 0.0f;
+  float da = ha ? d[pa_] : 0.0f, db = hb ? d[pb_] : 0.0f;
   int j = lg.j[g], total = lg.total[g], in_slice = lg.in_slice[g];
-  double left = lg.left[g], right = lg.right[g], t = lg.t[g], alpha = lg.alpha[g];
-  float logL0 = lg.logL0[g];
+  float left = lg.left[g], right = lg.right[g], t = lg.t[g], alpha = lg.alpha[g], logL0 = lg.logL0[g];
   Key ck = {lg.ck[2 * g], lg.ck[2 * g + 1]};
   Key after_key = {lg.after_key[2 * g], lg.after_key[2 * g + 1]};
   Key dir_key = {lg.dir_key[2 * g], lg.dir_key[2 * g + 1]};
@@ -133,15 +160,15 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
     const bool accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
     if (accept || in_slice >= b.max_evals_per_slice) {
       if (!accept) flags |= LG_FAILED;
-      ua = __dadd_rn(ua, __dmul_rn(t, da));
-      ub = __dadd_rn(ub, __dmul_rn(t, db));
+      pair_add(ua, fmaf(t, da, la), ua, la);
+      pair_add(ub, fmaf(t, db, lb), ub, lb);
       u_changed = true;
       logL0 = logL;
       const int ph = j - (S - 1 - K);
       if (K > 0 && ph >= 0 && j < S - 1) {
         double *phU = (double *)(b.ph_U + rd.phU_off) + ((size_t)c * K + ph) * P;
-        if (ha) phU[pa_] = ua;
-        if (hb) phU[pb_] = ub;
+        if (ha) phU[pa_] = (double)ua + (double)la;
+        if (hb) phU[pb_] = (double)ub + (double)lb;
         if (lane == 0) b.ph_L[rd.phL_off + (size_t)c * K + ph] = logL;
       }
       ++j;
@@ -159,8 +186,8 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
   }
   if (flags & LG_DONE) {
     double *nu = (double *)(b.new_U + rd.newU_off) + (size_t)c * P;
-    if (ha) nu[pa_] = ua;
-    if (hb) nu[pb_] = ub;
+    if (ha) nu[pa_] = (double)ua + (double)la;
+    if (hb) nu[pb_] = (double)ub + (double)lb;
     if (lane == 0) {
       b.new_L[rd.shell_off + c] = logL0;
       b.new_E[rd.shell_off + c] = total;
@@ -170,13 +197,13 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
   } else {
     if (flags & LG_NEED_DIR) {
       if (P == 1) {
-        da = 1.0;
+        da = 1.0f;
       } else {
         const float va = ha ? normal_from_bits(bits64(dir_key, (uint32_t)pa_)) : 0.0f;
         const float vb = hb ? normal_from_bits(bits64(dir_key, (uint32_t)pb_)) : 0.0f;
-        const double inv = 1.0 / sqrt((double)warp_sum(fmaf(va, va, vb * vb)));
-        da = (double)va * inv;
-        db = (double)vb * inv;
+        const float nrm = sqrtf(warp_sum(fmaf(va, va, vb * vb)));
+        da = va / nrm;
+        db = vb / nrm;
       }
       d_changed = true;
       flags &= ~LG_NEED_DIR;
@@ -188,43 +215,45 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
     if (start) {
       after_key = fold(B, 3u);
       alpha = lg_alpha(j, S);
-      double t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
+      // chord of u0 + t d in the unit cube; 1 - u = (1 - a) - b keeps the tails exact
+      float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const bool have = h ? hb : ha;
         if (have) {
-          const double uu = h ? ub : ua, dd = h ? db : da;
-          const double t1 = (1.0 - uu) / dd, t0 = -uu / dd;
-          t1r = fmin(t1r, t1 >= 0.0 ? t1 : INFINITY);
-          t1l = fmax(t1l, t1 <= 0.0 ? t1 : -INFINITY);
-          t0r = fmin(t0r, t0 >= 0.0 ? t0 : INFINITY);
-          t0l = fmax(t0l, t0 <= 0.0 ? t0 : -INFINITY);
+          const float uu = h ? ub : ua, ll = h ? lb : la, dd = h ? db : da;
+          const float t1 = ((1.0f - uu) - ll) / dd, t0 = -(uu + ll) / dd;
+          t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
+          t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
+          t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
+          t0l = fmaxf(t0l, t0 <= 0.f ? t0 : -INFINITY);
         }
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        t1r = fmin(t1r, __shfl_xor_sync(0xffffffffu, t1r, o));
-        t1l = fmax(t1l, __shfl_xor_sync(0xffffffffu, t1l, o));
-        t0r = fmin(t0r, __shfl_xor_sync(0xffffffffu, t0r, o));
-        t0l = fmax(t0l, __shfl_xor_sync(0xffffffffu, t0l, o));
+        t1r = fminf(t1r, __shfl_xor_sync(0xffffffffu, t1r, o));
+        t1l = fmaxf(t1l, __shfl_xor_sync(0xffffffffu, t1l, o));
+        t0r = fminf(t0r, __shfl_xor_sync(0xffffffffu, t0r, o));
+        t0l = fmaxf(t0l, __shfl_xor_sync(0xffffffffu, t0l, o));
       }
-      right = fmin(t0r, t1r);
-      left = fmax(t0l, t1l);
+      right = fminf(t0r, t1r);
+      left = fmaxf(t0l, t1l);
       in_slice = 0;
     } else {
-      if (t < 0.0) left = t;
-      if (t > 0.0) right = t;
+      if (t < 0.f) left = t;
+      if (t > 0.f) right = t;
       if (rd.midpoint) {
-        if (t < 0.0) left = __dmul_rn(alpha, left);
-        if (t > 0.0) right = __dmul_rn(alpha, right);
+        if (t < 0.f) left = alpha * left;
+        if (t > 0.f) right = alpha * right;
       }
     }
     // _pick_point_in_interval (uni_slice_sampler.py:67-89): t = left + u (right - left)
-    t = __dadd_rn(left, __dmul_rn(uniform01_d(bits64(tk, 0u)), __dsub_rn(right, left)));
+    t = fmaf(uniform01(bits64(tk, 0u)), right - left, left);
     const int *kind = b.prior_kind + rd.prior_off;
     const float *pa = b.prior_a + rd.prior_off, *pb = b.prior_b + rd.prior_off;
-    const float wa = ha ? prior_quantile_d(kind[pa_], pa[pa_], pb[pa_], __dadd_rn(ua, __dmul_rn(t, da))) : 0.0f;
-    const float wb = hb ? prior_quantile_d(kind[pb_], pa[pb_], pb[pb_], __dadd_rn(ub, __dmul_rn(t, db))) : 0.0f;
+    // proposal u0 + t d = a + (b + t d): the step goes into the low part
+    const float wa = ha ? prior_quantile_pair(kind[pa_], pa[pa_], pb[pa_], ua, fmaf(t, da, la)) : 0.0f;
+    const float wb = hb ? prior_quantile_pair(kind[pb_], pa[pb_], pb[pb_], ub, fmaf(t, db, lb)) : 0.0f;
     if (lg.use_tc) {
       float *wh = lg.W_hi + (size_t)g * 64, *wl = lg.W_lo + (size_t)g * 64;
       if (ha) tf32_split(wa, wh[pa_], wl[pa_]);
@@ -235,10 +264,17 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
       if (hb) W[pb_] = wb;
     }
     flags |= LG_PENDING;
+    if (lane == 0 && lg.tile_pending) lg.tile_pending[lg.tile_base[r] + (c >> 7)] = 1;
   }
   if (u_changed) {
-    if (ha) u0[pa_] = ua;
-    if (hb) u0[pb_] = ub;
+    if (ha) {
+      u0[pa_] = ua;
+      u0l[pa_] = la;
+    }
+    if (hb) {
+      u0[pb_] = ub;
+      u0l[pb_] = lb;
+    }
   }
   if (d_changed) {
     if (ha) d[pa_] = da;
@@ -463,8 +499,9 @@ int lg_check(const gbns_batch *batch, const gbns_lg_bufs *lg) {
       !lg->ss || !lg->W || !lg->u0 || !lg->dir || !lg->chains_left)
     return lg_fail(-1, "gbns_lg: bad arguments (1 <= pmax <= 64, chain buffers required)");
   if (lg->use_tc && (!lg->W_hi || !lg->W_lo || !lg->Phi_hi || !lg->Phi_lo || !lg->row_base || lg->total_rows < 1 ||
-                     lg->num_items_tc < 0 || (lg->num_items_tc > 0 && !lg->items_tc)))
-    return lg_fail(-1, "gbns_lg: use_tc needs W_hi, W_lo, Phi_hi, Phi_lo, row_base and items_tc");
+                     lg->num_items_tc < 0 || lg->num_ctas_tc < 0 || (lg->num_items_tc > 0 && !lg->items_tc) ||
+                     !lg->tile_base || !lg->tile_pending || !lg->tc_done || lg->num_tiles < 0))
+    return lg_fail(-1, "gbns_lg: use_tc needs W_hi, W_lo, Phi_hi, Phi_lo, row_base, items_tc and num_ctas_tc >= 0");
   return 0;
 }
 }  // namespace

@@ -1,7 +1,7 @@
 // gbns_phiw_tc.cu -- the Phi w residual contraction on the 5th-generation tensor cores.
 //
-// For a tile of 128 points (slice proposals, or dead points for the adjoint) and 256 data
-// rows, D[point][row] = w_point . Phi_row is one tcgen05 GEMM with K = P <= 64:
+// For a tile of 128 points (slice proposals, or dead points for the adjoint) and 128 / 256
+// data rows, D[point][row] = w_point . Phi_row is one tcgen05 GEMM with K = P <= 64:
 //   * w and Phi are held as TF32 hi + lo parts (x = hi + lo, both rounded to TF32), rows
 //     padded with zeros to a multiple of 32 floats, so one K block is one 128-byte row;
 //   * one thread issues the TMA loads of the four K-major tiles (128B swizzle, one mbarrier
@@ -228,23 +228,289 @@ __device__ void tc_resid_tile(const TcMaps &maps, int a_row, int b_row, int nkb,
   }
 }
 
-// Sampler step: the pending proposals of each (run, 128-chain tile, 256-row tile) item.
-__global__ void __launch_bounds__(128) k_lg_resid_tc(const __grid_constant__ TcMaps maps, gbns_batch b,
-                                                     gbns_lg_bufs lg) {
-  const int *it = lg.items_tc + 4 * (size_t)blockIdx.x;
-  const int r = it[0], c0 = it[1], nc = it[2], row0 = it[3];
-  const gbns_run_desc &rd = b.runs[r];
-  gbns_run_state &st = b.state[r];
-  if (st.done || st.phase != 1) return;
-  // skip the tile when none of its chains has a pending proposal (finished chains keep
-  // stepping in lock step with the slowest chain of the batch)
-  const int t = threadIdx.x;
-  const bool pending = t < nc && (lg.flags[rd.shell_off + c0 + t] & LG_PENDING) != 0;
-  if (!__syncthreads_or(pending)) return;
-  const int P = rd.D, N = rd.N;
-  const float *y = b.fparams + rd.param_off + (size_t)N * P;
-  tc_resid_tile(maps, (int)(rd.shell_off + c0), (int)(lg.row_base[r] + row0), (P + TC_KB - 1) / TC_KB, (P + 7) / 8,
-                nc, min(TC_N, N - row0), y + row0, lg.ss + rd.shell_off + c0, nullptr, &st.status);
+// ------------------------------------------------------------------ sampler step
+//
+// Persistent, warp-specialised: each CTA walks work units (run, 128-chain tile, range of
+// 128-row tiles) with a grid stride.  Warp 0 streams the unit's W tile (hi / lo) and its Phi
+// row tiles (hi / lo) through shared memory with TMA, warp 1 issues the 3xTF32 MMAs of each
+// row tile into a ring of 128-column accumulators in tensor memory, and warps 2-5 drain the
+// accumulators (thread = chain), keep the chain's partial sum of squares in a register over
+// the unit's row tiles and add it to the chain's FP64 total once per unit.  Copies, MMAs and
+// epilogue of successive row tiles overlap.  Units whose chain tile has no pending proposal
+// are skipped by every role alike (the flags are read-only during the launch).
+constexpr int SR_ROWS = 128;                       // data rows per tile (accumulator columns)
+constexpr unsigned SR_BOX = 128 * TC_KB * 4;       // one K block of 128 rows: 16 KB
+constexpr int SR_THREADS = 192;
+constexpr uint32_t SR_IDESC = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(SR_ROWS >> 3) << 17) |
+                              ((uint32_t)(TC_M >> 4) << 24);
+
+struct alignas(128) SrMaps {
+  CUtensorMap w_hi, w_lo, phi_hi, phi_lo;
+};
+
+__device__ __forceinline__ void tc_mma_d(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
+// Bounded wait that also gives up as soon as another role has aborted.
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity, const volatile int *abort_flag) {
+  const long long t0 = clock64();
+  while (true) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (*abort_flag) return false;
+    if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+  }
+}
+
+// Work unit u: false if the run is inactive or the chain tile has no pending proposal (the
+// chain step marks such tiles; every warp reaches the same answer).
+__device__ __forceinline__ bool sr_unit(const gbns_batch &b, const gbns_lg_bufs &lg, int u, int lane, int &r, int &c0,
+                                        int &rt0, int &nrt) {
+  const int *it = lg.items_tc + 4 * (size_t)u;
+  r = it[0];
+  c0 = it[1];
+  rt0 = it[2];
+  nrt = it[3];
+  const gbns_run_state &st = b.state[r];
+  if (st.done || st.phase != 1) return false;
+  return __shfl_sync(0xffffffffu, lg.tile_pending[lg.tile_base[r] + (c0 >> 7)], 0) != 0;
+}
+
+__global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constant__ SrMaps maps, gbns_batch b,
+                                                            gbns_lg_bufs lg, int nkb_max, int acc_stages) {
+  extern __shared__ unsigned char sr_dyn[];
+  // 0 w_full, 1 w_empty, 2-3 phi_full, 4-5 phi_empty, 6-9 acc_full, 10-13 acc_empty
+  __shared__ __align__(8) unsigned long long bars[14];
+  __shared__ uint32_t tmem_slot;
+  __shared__ int abort_flag;
+  __shared__ float ys[4][SR_ROWS];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t base = (smem_u32(sr_dyn) + 1023u) & ~1023u;
+  const int NK = nkb_max;
+  auto w_hi = [&](int kb) { return base + (uint32_t)kb * SR_BOX; };
+  auto w_lo = [&](int kb) { return base + (uint32_t)(NK + kb) * SR_BOX; };
+  auto phi_hi = [&](int p, int kb) { return base + (uint32_t)(2 * NK + p * 2 * NK + kb) * SR_BOX; };
+  auto phi_lo = [&](int p, int kb) { return base + (uint32_t)(2 * NK + p * 2 * NK + NK + kb) * SR_BOX; };
+  auto bar = [&](int q) { return smem_u32(&bars[q]); };
+
+  if (tid == 0) {
+    mbar_init(bar(0), 1);
+    mbar_init(bar(1), 1);
+    for (int q = 2; q < 6; ++q) mbar_init(bar(q), 1);
+    for (int q = 0; q < 4; ++q) {
+      mbar_init(bar(6 + q), 1);
+      mbar_init(bar(10 + q), 4);  // one arrival per epilogue warp
+    }
+    abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncwarp();
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"((uint32_t)(acc_stages * SR_ROWS))
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const volatile int *ab = &abort_flag;
+  const int nunits = lg.num_items_tc;
+
+  if (warp == 0) {
+    // ---- producer: W tile per unit, Phi hi / lo per row tile (two stages)
+    int wuse = 0, pt = 0;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+      int r, c0, rt0, nrt;
+      if (!sr_unit(b, lg, u, lane, r, c0, rt0, nrt)) continue;
+      const gbns_run_desc &rd = b.runs[r];
+      const int nkb = (rd.D + TC_KB - 1) / TC_KB;
+      const int brow = (int)lg.row_base[r];
+      int failed = 0;
+      if (lane == 0) {
+        // Phi row tile t into the next stage (waits until the MMAs have released it)
+        auto load_phi = [&](int t) -> bool {
+          const int p = pt & 1;
+          if (!mbar_wait_or_abort(bar(4 + p), (uint32_t)(((pt >> 1) & 1) ^ 1), ab)) return false;
+          mbar_expect_tx(bar(2 + p), 2u * (uint32_t)nkb * SR_BOX);
+          const int y0 = brow + (rt0 + t) * SR_ROWS;
+          for (int kb = 0; kb < nkb; ++kb) {
+            tma_load_2d(phi_hi(p, kb), &maps.phi_hi, kb * TC_KB, y0, bar(2 + p));
+            tma_load_2d(phi_lo(p, kb), &maps.phi_lo, kb * TC_KB, y0, bar(2 + p));
+          }
+          ++pt;
+          return true;
+        };
+        // the first Phi tile goes before the W tile, so it streams while the previous
+        // unit's last MMAs (which hold the W buffer) finish
+        if (!load_phi(0) || !mbar_wait_or_abort(bar(1), (uint32_t)((wuse & 1) ^ 1), ab)) {
+          failed = 1;
+        } else {
+          mbar_expect_tx(bar(0), 2u * (uint32_t)nkb * SR_BOX);
+          const int ar = (int)(rd.shell_off + c0);
+          for (int kb = 0; kb < nkb; ++kb) {
+            tma_load_2d(w_hi(kb), &maps.w_hi, kb * TC_KB, ar, bar(0));
+            tma_load_2d(w_lo(kb), &maps.w_lo, kb * TC_KB, ar, bar(0));
+          }
+          for (int t = 1; t < nrt; ++t)
+            if (!load_phi(t)) {
+              failed = 1;
+              break;
+            }
+        }
+        if (failed) {
+          abort_flag = 1;
+          atomicOr(&b.state[r].status, (int)GBNS_ERR_WAIT_TIMEOUT);
+        }
+      }
+      ++wuse;
+      if (__shfl_sync(0xffffffffu, failed, 0)) break;
+      pt = __shfl_sync(0xffffffffu, pt, 0);
+    }
+  } else if (warp == 1) {
+    // ---- MMA issuer
+    int wuse = 0, pt = 0, at = 0;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+      int r, c0, rt0, nrt;
+      if (!sr_unit(b, lg, u, lane, r, c0, rt0, nrt)) continue;
+      const gbns_run_desc &rd = b.runs[r];
+      const int nk8 = (rd.D + 7) / 8;
+      int failed = 0;
+      if (lane == 0) {
+        if (!mbar_wait_or_abort(bar(0), (uint32_t)(wuse & 1), ab)) failed = 1;
+        for (int t = 0; t < nrt && !failed; ++t, ++pt, ++at) {
+          const int p = pt & 1, a = at % acc_stages;
+          if (!mbar_wait_or_abort(bar(2 + p), (uint32_t)((pt >> 1) & 1), ab) ||
+              !mbar_wait_or_abort(bar(10 + a), (uint32_t)(((at / acc_stages) & 1) ^ 1), ab)) {
+            failed = 1;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t d = tmem + (uint32_t)(a * SR_ROWS);
+          for (int k8 = 0; k8 < nk8; ++k8) {
+            const int kb = k8 >> 2;
+            const uint32_t off = (uint32_t)(k8 & 3) * 32u;
+            const uint64_t ah = smem_desc(w_hi(kb) + off), al = smem_desc(w_lo(kb) + off);
+            const uint64_t bh = smem_desc(phi_hi(p, kb) + off), bl = smem_desc(phi_lo(p, kb) + off);
+            tc_mma_d(d, al, bh, SR_IDESC, k8 > 0 ? 1u : 0u);
+            tc_mma_d(d, ah, bl, SR_IDESC, 1u);
+            tc_mma_d(d, ah, bh, SR_IDESC, 1u);
+          }
+          tc_commit(bar(6 + a));   // accumulator a full
+          tc_commit(bar(4 + p));   // Phi stage p free
+          if (t == nrt - 1) tc_commit(bar(1));  // W tile free
+        }
+        if (failed) {
+          abort_flag = 1;
+          atomicOr(&b.state[r].status, (int)GBNS_ERR_WAIT_TIMEOUT);
+        }
+      }
+      ++wuse;
+      if (__shfl_sync(0xffffffffu, failed, 0)) break;
+      pt = __shfl_sync(0xffffffffu, pt, 0);
+      at = __shfl_sync(0xffffffffu, at, 0);
+    }
+  } else {
+    // ---- epilogue: warps 2-5 own tensor-memory lane quarters 2, 3, 0, 1
+    const int q = warp & 3, ew = warp - 2;
+    int at = 0;
+    for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
+      int r, c0, rt0, nrt;
+      if (!sr_unit(b, lg, u, lane, r, c0, rt0, nrt)) continue;
+      const gbns_run_desc &rd = b.runs[r];
+      const int N = rd.N;
+      const float *y = b.fparams + rd.param_off + (size_t)N * rd.D;
+      double ssum = 0.0;
+      bool ok = true;
+      // y of the next row tile is loaded into registers while the current one is processed
+      float yn[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int row = rt0 * SR_ROWS + lane + 32 * k;
+        yn[k] = row < N ? y[row] : 0.0f;
+      }
+      for (int t = 0; t < nrt; ++t, ++at) {
+        const int a = at % acc_stages;
+        const int row0 = (rt0 + t) * SR_ROWS;
+        const int nrows = min(SR_ROWS, N - row0);
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ys[ew][lane + 32 * k] = yn[k];
+        __syncwarp();
+        if (t + 1 < nrt) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            const int row = row0 + SR_ROWS + lane + 32 * k;
+            yn[k] = row < N ? y[row] : 0.0f;
+          }
+        }
+        ok = mbar_wait_or_abort(bar(6 + a), (uint32_t)((at / acc_stages) & 1), ab);
+        ok = __all_sync(0xffffffffu, ok);
+        if (!ok) break;
+        tc_fence_after();
+        const uint32_t taddr = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * SR_ROWS);
+        const int nch = (nrows + 31) >> 5;
+        float part = 0.0f;
+        for (int ch = 0; ch < nch; ++ch) {
+          float v[32];
+          tc_ld32(taddr + (uint32_t)(ch * 32), v);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            const float rr = ys[ew][ch * 32 + j] - v[j];
+            part = (ch * 32 + j < nrows) ? fmaf(rr, rr, part) : part;
+          }
+        }
+        ssum += (double)part;
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(bar(10 + a));  // accumulator a drained
+      }
+      if (!ok) {
+        if (lane == 0) {
+          abort_flag = 1;
+          atomicOr(&b.state[r].status, (int)GBNS_ERR_WAIT_TIMEOUT);
+        }
+        break;
+      }
+      const int c = c0 + q * 32 + lane;
+      if (c < rd.s) atomicAdd(&lg.ss[rd.shell_off + c], ssum);
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"((uint32_t)(acc_stages * SR_ROWS))
+                 : "memory");
+  }
+  // the last CTA to finish clears the pending-tile marks for the next chain step
+  __shared__ int last;
+  if (tid == 0) {
+    __threadfence();
+    last = atomicAdd(lg.tc_done, 1) == (int)gridDim.x - 1;
+  }
+  __syncthreads();
+  if (last) {
+    for (int q = tid; q < lg.num_tiles; q += blockDim.x) lg.tile_pending[q] = 0;
+    if (tid == 0) *lg.tc_done = 0;
+  }
 }
 
 // Adjoint: all dead points (blockIdx.x: 128-point tile) against all rows (blockIdx.y).
@@ -256,7 +522,7 @@ __global__ void __launch_bounds__(128) k_adj_resid_tc(const __grid_constant__ Tc
                 min(TC_N, N - row0), y + row0, ss + p0, ry + p0, status);
 }
 
-// Phi of every run -> TF32 hi/lo rows of 64 floats (zero beyond P).
+// Phi of every run -> TF32 hi / lo rows of 64 floats (zero beyond P).
 __global__ void k_split_phi(gbns_batch b, gbns_lg_bufs lg) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= lg.total_rows * 64) return;
@@ -343,7 +609,7 @@ cudaError_t set_smem_attrs() {
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(mu);
   if (done[dev]) return cudaSuccess;
-  const int bytes = 2 * (int)TC_KB_BYTES + 1024;
+  const int bytes = 2 * (int)TC_KB_BYTES + 1024;  // two K blocks: 6 x 2 x 16 KB (sampler) or 2 x 96 KB (adjoint)
   err = cudaFuncSetAttribute(k_lg_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (err == cudaSuccess) err = cudaFuncSetAttribute(k_adj_resid_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (err == cudaSuccess) done[dev] = true;
@@ -365,21 +631,27 @@ cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStrea
 cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t s) {
   cudaError_t e = set_smem_attrs();
   if (e != cudaSuccess) return e;
-  TcMaps maps;
-  if (!encode_rows(&maps.a_hi, lg.W_hi, lg.total_chains, 64, TC_M) ||
-      !encode_rows(&maps.a_lo, lg.W_lo, lg.total_chains, 64, TC_M) ||
-      !encode_rows(&maps.b_hi, lg.Phi_hi, lg.total_rows, 64, TC_N) ||
-      !encode_rows(&maps.b_lo, lg.Phi_lo, lg.total_rows, 64, TC_N))
+  SrMaps maps;
+  if (!encode_rows(&maps.w_hi, lg.W_hi, lg.total_chains, 64, 128) ||
+      !encode_rows(&maps.w_lo, lg.W_lo, lg.total_chains, 64, 128) ||
+      !encode_rows(&maps.phi_hi, lg.Phi_hi, lg.total_rows, 64, 128) ||
+      !encode_rows(&maps.phi_lo, lg.Phi_lo, lg.total_rows, 64, 128))
     return cudaErrorInvalidValue;
+  // shared memory: W tile + two Phi stages, hi and lo, nkb K blocks each (96 KB per block);
+  // tensor memory: 4 accumulators of 128 columns at one CTA per SM, 2 at two CTAs per SM
   const int nkb = lg.pmax > TC_KB ? 2 : 1;
-  if (steps < 0) {
-    if (lg.num_items_tc > 0) k_lg_resid_tc<<<lg.num_items_tc, 128, nkb * TC_KB_BYTES + 1024, s>>>(maps, b, lg);
-    return cudaGetLastError();
-  }
-  for (int q = 0; q < steps; ++q) {
-    e = launch_lg_step_kernel(b, lg, s);
-    if (e != cudaSuccess) return e;
-    if (lg.num_items_tc > 0) k_lg_resid_tc<<<lg.num_items_tc, 128, nkb * TC_KB_BYTES + 1024, s>>>(maps, b, lg);
+  const unsigned smem = (unsigned)nkb * 6u * SR_BOX + 1024u;
+  const int per_sm = nkb == 1 ? 2 : 1, acc_stages = nkb == 1 ? 2 : 4;
+  int dev = 0, sms = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  int grid = sms * per_sm;
+  if (lg.num_ctas_tc > 0 && lg.num_ctas_tc < grid) grid = lg.num_ctas_tc;
+  if (grid > lg.num_items_tc) grid = lg.num_items_tc;
+  const int launches = steps < 0 ? 1 : steps;
+  for (int q = 0; q < launches; ++q) {
+    if (steps >= 0 && (e = launch_lg_step_kernel(b, lg, s)) != cudaSuccess) return e;
+    if (grid > 0) k_lg_resid_tc<<<grid, SR_THREADS, smem, s>>>(maps, b, lg, nkb, acc_stages);
   }
   return cudaGetLastError();
 }

@@ -281,16 +281,17 @@ class NSBatch:
         z = lambda n, dt=torch.float32: torch.zeros(max(n, 1), dtype=dt, device=dev)
         f64 = torch.float64
         self.lg_t = dict(j=z(nc, torch.int32), in_slice=z(nc, torch.int32), total=z(nc, torch.int32),
-                         flags=z(nc, torch.int32), left=z(nc, f64), right=z(nc, f64), t=z(nc, f64),
-                         alpha=z(nc, f64), logL0=z(nc), ck=z(2 * nc, torch.int32), after_key=z(2 * nc, torch.int32),
-                         slices_key=z(2 * nc, torch.int32), dir_key=z(2 * nc, torch.int32), u0=z(nd, f64),
-                         dir=z(nd, f64), W=z(nd), ss=z(nc, f64), chains_left=z(len(specs), torch.int32))
+                         flags=z(nc, torch.int32), left=z(nc), right=z(nc), t=z(nc), alpha=z(nc), logL0=z(nc),
+                         ck=z(2 * nc, torch.int32), after_key=z(2 * nc, torch.int32),
+                         slices_key=z(2 * nc, torch.int32), dir_key=z(2 * nc, torch.int32), u0=z(nd), u0_lo=z(nd),
+                         dir=z(nd), W=z(nd), ss=z(nc, f64), chains_left=z(len(specs), torch.int32))
         items = []
         for r, s in enumerate(specs):
             for c0 in range(0, s.shell_size, 64):
                 for row0 in range(0, s.N, 64):
                     items.append((r, c0, min(64, s.shell_size - c0), row0))
         self.lg_items = torch.tensor(np.array(items, np.int32).reshape(-1, 4), device=dev)
+        self.lg_t["chain_run"] = torch.tensor(np.repeat(np.arange(len(specs), dtype=np.int32), ss), device=dev)
         g = _ffi.LGBufs()
         for k, v in self.lg_t.items():
             setattr(g, k, v.data_ptr())
@@ -304,16 +305,23 @@ class NSBatch:
             Ns = np.array([s.N for s in specs], np.int64)
             row_base = np.concatenate([[0], np.cumsum(Ns)[:-1]]).astype(np.int64)
             rows = int(Ns.sum())
-            items_tc = []
-            for r, s in enumerate(specs):
-                for c0 in range(0, s.shell_size, 128):
-                    for row0 in range(0, s.N, 256):
-                        items_tc.append((r, c0, min(128, s.shell_size - c0), row0))
+            # work units (run, 128-chain tile, first 128-row tile, row tiles): row ranges sized so
+            # that there are about two units per CTA slot; the chain tiles of one row range are
+            # adjacent, so the CTAs that share its Phi tiles run together
+            tiles = [((s.shell_size + 127) // 128, (s.N + 127) // 128) for s in specs]
+            work = sum(ct * rt for ct, rt in tiles)
+            rs = max(1, min(16, work // (2 * 2 * 152)))
+            items_tc = [(r, c0, rt0, min(rs, rt - rt0)) for r, (ct, rt) in enumerate(tiles)
+                        for rt0 in range(0, rt, rs) for c0 in range(0, ct * 128, 128)]
             self.lg_tc_t = dict(W_hi=z(nc * 64), W_lo=z(nc * 64), Phi_hi=z(rows * 64), Phi_lo=z(rows * 64),
                                 row_base=torch.tensor(row_base, device=dev),
                                 items_tc=torch.tensor(np.array(items_tc, np.int32).reshape(-1, 4), device=dev))
+            tile_base = np.concatenate([[0], np.cumsum([ct for ct, _ in tiles])[:-1]]).astype(np.int32)
+            self.lg_tc_t.update(tile_base=torch.tensor(tile_base, device=dev),
+                                tile_pending=z(sum(ct for ct, _ in tiles), torch.int32), tc_done=z(1, torch.int32))
             for k, v in self.lg_tc_t.items():
                 setattr(g, k, v.data_ptr())
+            g.num_tiles = int(sum(ct for ct, _ in tiles))
             g.num_items_tc = len(items_tc)
             g.total_rows = rows
             g.use_tc = 1
