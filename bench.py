@@ -445,11 +445,12 @@ def blr_workload(R: int, seed: int, name: str):
         N, P = int(N), int(P)
         g = np.random.default_rng([seed, r])
         Phi = g.standard_normal((N, P)).astype(np.float32)
-        y = (Phi.astype(np.float64) @ g.standard_normal(P) + sigma * g.standard_normal(N)).astype(np.float32)
+        w_true = g.standard_normal(P)
+        y = (Phi.astype(np.float64) @ w_true + sigma * g.standard_normal(N)).astype(np.float32)
         n = 1024 if name == "blr" else 25 * P
         H = float(blr_information(Phi.astype(np.float64), y.astype(np.float64), sigma, tau))
         out.append(dict(N=N, P=P, sigma=float(sigma), tau=float(tau), Phi=Phi, y=y, n=n,
-                        cap=int(n * (1.3 * H + 2 * P + 60)), H=H))
+                        cap=int(n * (1.3 * H + 2 * P + 60)), H=H, w_z=w_true / tau))
     return out
 
 
@@ -613,7 +614,13 @@ def main_blr(args):
                                  "tau": round(wl[r]["tau"], 3), "H": round(wl[r]["H"], 1), "dlogZ": float(dz[r]),
                                  "uncert": float(host[r, 1]), "reason": int(st["termination_reason"][r]),
                                  "samples": int(st["num_samples"][r]), "cap": int(b.specs[r].max_samples)}
-                                for r in np.argsort(-np.abs(dz))[:3]]}
+                                for r in np.argsort(-np.abs(dz))[:3]],
+                "per_problem": {"dlogZ": [round(float(v), 4) for v in dz],
+                                "log_Z_uncert": [round(float(v), 4) for v in host[:, 1]],
+                                "grad_err": [[round(float(v), 4) for v in row] for row in gerr],
+                                "grad_mc_se": [[round(float(v), 4) for v in row] for row in se],
+                                "termination_reason": [int(v) for v in st["termination_reason"]],
+                                "max_abs_prior_z": [round(float(np.max(np.abs(p["w_z"]))), 3) for p in wl]}}
 
     # residual-kernel roofline: events inside the lock-step graph around every residual launch
     # over the first iterations of a fresh pass; algorithmic flops 2 N P per evaluation
