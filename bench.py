@@ -219,6 +219,8 @@ def main():
                     help="config3: keep only runs of this dimension (repeated to --runs); for kernel profiling")
     ap.add_argument("--plain-problems", type=int, default=4,
                     help="blr workloads: problems in the plain GPU + finite-difference comparison")
+    ap.add_argument("--no-e2e", action="store_true",
+                    help="blr workloads: skip the end-to-end pass (one more full step)")
     ap.add_argument("--kernel-profile", action="store_true",
                     help="blr workloads: init + --iterations NS iterations only (for ncu)")
     ap.add_argument("--cuda-core", action="store_true",
@@ -651,16 +653,18 @@ def main_blr(args):
 
     # end-to-end: Phi, y, sigma and the run table from pinned host memory, per-problem
     # (log Z, uncertainty, log Z(theta), gradient) back to the host
-    barrier()
-    e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0_.record()
-    for _ in range(args.steps):
-        host_out, h2d = step(from_host=True)
-    e1_.record()
-    barrier()
-    e2e_ms = e0_.elapsed_time(e1_)
-    e2e = {"value": R * args.steps * world / (e2e_ms / 1e3), "unit": "problems/s", "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": int(R * 5 * 8)}
+    e2e = None
+    if not args.no_e2e:
+        barrier()
+        e0_, e1_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0_.record()
+        for _ in range(args.steps):
+            host_out, h2d = step(from_host=True)
+        e1_.record()
+        barrier()
+        e2e_ms = e0_.elapsed_time(e1_)
+        e2e = {"value": R * args.steps * world / (e2e_ms / 1e3), "unit": "problems/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": int(R * 5 * 8)}
 
     line = {"metric": METRIC, "value": value, "unit": "problems/s (NS run + adjoint)", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
