@@ -24,6 +24,7 @@
  *   gbns_random_bits64 / gbns_uniform / gbns_normal <- jax.random.bits/uniform/normal (test hooks)
  *   gbns_count_crossed_edges <- count_crossed_edges       internals/tree_structure.py:33-108
  *   gbns_evidence_stats   <- compute_evidence_stats       internals/shrinkage_statistics.py:131-157
+ *   gbns_sample_evidence  <- sample_evidence              utils.py:433-484
  *   gbns_lg_shell_begin / gbns_lg_steps / gbns_lg_prepare_tc
  *                         <- _collect_shell + UniDimSliceSampler for a linear-Gaussian model
  *                            (the user likelihood N(y; Phi w, sigma^2 I), which a jaxns user
@@ -314,6 +315,11 @@ int gbns_evidence_adjoint_tc(const double *U_dev, const double *log_w_dev, long 
                              const float *y_dev, int N, double log_tau, double log_sigma, double *out_dev,
                              double *ss_scratch_dev, double *ry_scratch_dev, float *w_scratch_dev,
                              float *phi_scratch_dev, int *status_dev, void *stream);
+/* sample_evidence (utils.py:433-484): S replicas of log Z with the shrinkage T_i ~ Beta(n_i, 1)
+ * drawn from the jax key (key_dev: 2 words); num_live, log_L: the sorted samples' live-point
+ * counts and log-likelihoods (FP64), M < 2^32; log_Z_dev: [S]. */
+int gbns_sample_evidence(const uint32_t *key_dev, const int *num_live_dev, const double *log_L_dev, long long M,
+                         int S, double *log_Z_dev, void *stream);
 int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,
                         int nmax, gbns_evcalc *final_dev, double *log_X_mean_dev, double *log_dZ_mean_dev,
                         double *log_Z_mean_dev, void *stream);

@@ -9,5 +9,6 @@ from .public import (TerminationCondition, NestedSamplerResults, NestedSampler, 
                      UniDimSliceSampler, UniformSampler, ShardedStaticNestedSampler, NestedSamplerState,
                      round_up_num_live_points, round_up_max_samples)
 from . import random
+from .utils import sample_evidence, save_results, load_results, save_pytree, load_pytree
 
 __version__ = "0.1.0"

@@ -86,7 +86,8 @@ EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2
             "gbns_batch_finalize", "gbns_batch_results", "gbns_slice_shell", "gbns_count_crossed_edges",
             "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
             "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint",
-            "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc", "gbns_lg_chain_step", "gbns_lg_residual")
+            "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc", "gbns_lg_chain_step", "gbns_lg_residual",
+            "gbns_sample_evidence")
 
 _lib = None
 

@@ -173,4 +173,13 @@ int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long lo
                "gbns_evidence_stats");
 }
 
+int gbns_sample_evidence(const uint32_t *key_dev, const int *num_live_dev, const double *log_L_dev, long long M,
+                         int S, double *log_Z_dev, void *stream) {
+  if (M < 0 || M > 4294967295ll || S < 0 || !key_dev || (S > 0 && !log_Z_dev) ||
+      (M > 0 && (!num_live_dev || !log_L_dev)))
+    return fail(-1, "gbns_sample_evidence: bad arguments%s");
+  return check(gbns::launch_sample_evidence(key_dev, num_live_dev, log_L_dev, M, S, log_Z_dev, (cudaStream_t)stream),
+               "gbns_sample_evidence");
+}
+
 }  // extern "C"

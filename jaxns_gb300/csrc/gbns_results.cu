@@ -271,6 +271,84 @@ __global__ void k_rng(int mode, const uint32_t *key, const uint32_t *counts, voi
   }
 }
 
+// sample_evidence (utils.py:433-484): S replicas of log Z with the shrinkage drawn.
+// Replica s (one CTA): u_i = uniform(split(split(key, S)[s], M)[i]), log T_i = log(u_i) / n_i,
+// log X_i = sum_{j<i} log T_j (FP64 block scan), and log Z = logsumexp_i(log X_i +
+// log(1 - T_i) + log L_i) -- the sequential LogSpace accumulation of the reference written
+// as a prefix sum and one log-sum-exp.
+__global__ void __launch_bounds__(1024) k_sample_evidence(const uint32_t *key, const int *__restrict__ num_live,
+                                                          const double *__restrict__ log_L, long long M,
+                                                          double *__restrict__ out) {
+  __shared__ double wsum[32];
+  __shared__ double red_m[32], red_s[32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, nw = blockDim.x >> 5;
+  const Key ks = fold(Key{key[0], key[1]}, (uint32_t)blockIdx.x);
+  double carry = 0.0;                  // log X at the start of the chunk
+  double m = -INFINITY, acc = 0.0;     // this thread's running log-sum-exp: m + log(acc)
+  for (long long base = 0; base < M; base += blockDim.x) {
+    const long long i = base + tid;
+    double lt = 0.0;
+    if (i < M) lt = log(uniform01_d(bits64(fold(ks, (uint32_t)i), 0u))) / (double)num_live[i];
+    // inclusive scan of lt over the block
+    double v = lt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double t = __shfl_up_sync(0xffffffffu, v, o);
+      if (lane >= o) v += t;
+    }
+    if (lane == 31) wsum[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      double w = lane < nw ? wsum[lane] : 0.0;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const double t = __shfl_up_sync(0xffffffffu, w, o);
+        if (lane >= o) w += t;
+      }
+      if (lane < nw) wsum[lane] = w;
+    }
+    __syncthreads();
+    const double before = (warp > 0 ? wsum[warp - 1] : 0.0) + (v - lt);  // exclusive prefix in the chunk
+    const double total = wsum[nw - 1];
+    if (i < M) {
+      // X_i (1 - T_i) L_i; T_i = 1 only if u_i rounds to 1, which the 52-bit uniform cannot
+      const double term = (carry + before) + log1p(-exp(lt)) + log_L[i];
+      if (term > m) {
+        acc = acc * exp(m - term) + 1.0;
+        m = term;
+      } else if (term > -INFINITY) {
+        acc += exp(term - m);
+      }
+    }
+    carry += total;
+    __syncthreads();
+  }
+  // combine the threads' (m, acc)
+  double gm = m;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) gm = fmax(gm, __shfl_xor_sync(0xffffffffu, gm, o));
+  if (lane == 0) red_m[warp] = gm;
+  __syncthreads();
+  gm = -INFINITY;
+  for (int q = 0; q < nw; ++q) gm = fmax(gm, red_m[q]);
+  double a = (m > -INFINITY) ? acc * exp(m - gm) : 0.0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+  if (lane == 0) red_s[warp] = a;
+  __syncthreads();
+  if (tid == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < nw; ++q) sum += red_s[q];
+    out[blockIdx.x] = (gm > -INFINITY) ? gm + log(sum) : -INFINITY;
+  }
+}
+
+cudaError_t launch_sample_evidence(const uint32_t *key, const int *num_live, const double *log_L, long long M, int S,
+                                   double *out, cudaStream_t stream) {
+  if (S > 0) k_sample_evidence<<<S, 1024, 0, stream>>>(key, num_live, log_L, M, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n,
                        cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;

@@ -488,6 +488,33 @@ void orc_linear_to_log_stats(double log_f_mean, double log_f2_mean, double *mu, 
     if (isnan(s)) *var = s;
 }
 
+/* sample_evidence (utils.py:433-484): S replicas of log Z with the shrinkage drawn instead
+ * of averaged.  Replica s: keys split(split(key, S)[s], M); per sample i, in order,
+ * log T = log(uniform(key_i)) / n_i (T ~ Beta(n_i, 1)), next X = X T,
+ * dZ = (X - next X) L_i in LogSpace (signed_logaddexp, log_semiring.py:28-48), Z += dZ. */
+void orc_sample_evidence(uint32_t k0, uint32_t k1, const long *num_live, const double *log_L, long M, int S,
+                         double *log_Z_out) {
+    okey key = {k0, k1};
+    for (int s = 0; s < S; ++s) {
+        okey ks = key_fold(key, (uint64_t)s);
+        double log_Z = -INFINITY, log_X = 0.0;
+        for (long i = 0; i < M; ++i) {
+            okey ki = key_fold(ks, (uint64_t)i);
+            double u = uniform_f64(ki, 0, 0.0, 1.0);
+            double log_T = log(u) / (double)num_live[i];
+            double log_nX = log_X + log_T;
+            /* X - next X: signed_logaddexp(log_X, +1, log_nX, -1) */
+            double delta = -fabs(log_nX - log_X);
+            double amax = log_X > log_nX ? log_X : log_nX;
+            double log_dX = isnan(delta) ? log_X + log_nX : amax + log1p(-exp(delta));
+            double log_dZ = log_dX + log_L[i];
+            log_Z = lae(log_Z, log_dZ);
+            log_X = log_nX;
+        }
+        log_Z_out[s] = log_Z;
+    }
+}
+
 /* ------------------------------------------------------- tree counting ---- */
 
 /* count_crossed_edges (internals/tree_structure.py:33-108).  num_samples < 0 means the

@@ -312,6 +312,18 @@ def _ev_tuple(e):
     return {f: getattr(e, f) for f in EV_FIELDS}
 
 
+def sample_evidence(key, num_live_points_per_sample, log_L_samples, S=100):
+    """utils.py:433-484 (sample_evidence), FP64."""
+    n = np.ascontiguousarray(num_live_points_per_sample, np.int64)
+    L = np.ascontiguousarray(log_L_samples, np.float64)
+    out = np.zeros(S, np.float64)
+    key = np.asarray(key, np.uint32)
+    lib().orc_sample_evidence(ctypes.c_uint32(int(key[0])), ctypes.c_uint32(int(key[1])),
+                              n.ctypes.data_as(ctypes.c_void_p), _dp(L), ctypes.c_long(len(L)), ctypes.c_int(S),
+                              _dp(out))
+    return out
+
+
 def compute_evidence_stats(log_L, num_live_points):
     log_L = np.ascontiguousarray(log_L, np.float64)
     nl = np.ascontiguousarray(num_live_points, np.float64)
