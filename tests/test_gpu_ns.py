@@ -164,3 +164,75 @@ def test_config2_shells(gpu_lib):
     res = ns.to_results(reason, state)
     truth = shells_log_Z()
     assert abs(res.log_Z_mean - truth) < 4 * res.log_Z_uncert + 0.05, (res.log_Z_mean, res.log_Z_uncert, truth)
+
+
+def test_phantoms_one_iteration_match_oracle(gpu_lib, oracle_mod):
+    """k = 3 phantoms per chain (uni_slice_sampler.py:430-441, add_phantom_samples_to_state
+    sharded_static.py:181-207): after one iteration the store holds the discarded shell and then
+    s*k phantoms (phantom flag set, sender = the shell's sender), matching the oracle."""
+    import jaxns_gb300 as gb
+    from jaxns_gb300.engine import NSBatch
+    D, n, S, K = 4, 256, 20, 3
+    model, mu, cov = _mvn_model(gb, D, 1)
+    ns = gb.NestedSampler(model, num_live_points=n * (K + 1), num_slices=S, k=K)
+    key = gb.random.PRNGKey(5)
+    spec = ns.nested_sampler.run_spec(key, ns.normalise_term_cond(gb.TerminationCondition(dlogZ=1e-4)))
+    assert spec.num_phantom == K and spec.num_live_points == n
+    b = NSBatch([spec])
+    b.init()
+    b.iterate(1)
+    torch.cuda.synchronize()
+    st = b.state()[0]
+    s = n // 2
+    assert int(st["num_samples"]) == s * (1 + K)
+    sv = b.store_view(0)
+    ph = sv["phantom"].cpu().numpy()
+    np.testing.assert_array_equal(ph[:s], 0)
+    np.testing.assert_array_equal(ph[s:s * (1 + K)], 1)
+    np.testing.assert_array_equal(sv["nevals"][s:s * (1 + K)].cpu().numpy(), 0)
+    om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    o = oracle_mod.ns_run(om, key, n, S, max_samples=spec.max_samples, num_phantom=K, term_cond={"dlogZ": 1e-4},
+                          max_iterations=1)
+    gL = sv["log_L"][s:s * (1 + K)].cpu().numpy()
+    oL = o.log_L[s:s * (1 + K)]
+    close = np.abs(gL - oL) <= 2e-3 + 2e-4 * np.abs(oL)
+    assert close.mean() >= 0.9, close.mean()
+    np.testing.assert_array_equal(np.array(st["key"], np.uint32), o.register["key"])
+
+
+def test_parameter_estimation_and_difficult_model_log_Z(gpu_lib):
+    """parameter_estimation (k = D phantoms) and difficult_model (no midpoint shrink, s = 10):
+    log Z within 4 sigma of the analytic value; phantom count = k / (k + 1) of the samples."""
+    import jaxns_gb300 as gb
+    D = 4
+    truth = -D * np.log(20.0)
+    for kw in (dict(parameter_estimation=True), dict(difficult_model=True)):
+        model, _, _ = _mvn_model(gb, D, 2)
+        ns = gb.NestedSampler(model, num_live_points=400, **kw)
+        reason, state = ns(gb.random.PRNGKey(8), gb.TerminationCondition(dlogZ=1e-4))
+        res = ns.to_results(reason, state)
+        assert abs(res.log_Z_mean - truth) < 4 * res.log_Z_uncert + 0.02, (kw, res.log_Z_mean, res.log_Z_uncert)
+        if kw.get("parameter_estimation"):
+            k = D
+            assert res.total_phantom_samples > 0
+            assert abs(res.total_phantom_samples / res.total_num_samples - k / (k + 1)) < 0.05
+
+
+def test_peak_XL_frac_termination_matches_oracle(gpu_lib, oracle_mod):
+    """TerminationCondition(peak_XL_frac) (termination.py:140-146): same iteration count and
+    termination bit as the oracle."""
+    import jaxns_gb300 as gb
+    from jaxns_gb300.engine import NSBatch
+    D, n = 3, 128
+    model, mu, cov = _mvn_model(gb, D, 4)
+    ns = gb.NestedSampler(model, num_live_points=n, num_slices=4 * D)
+    key = gb.random.PRNGKey(12)
+    tc = gb.TerminationCondition(peak_XL_frac=0.01)
+    spec = ns.nested_sampler.run_spec(key, ns.normalise_term_cond(tc))
+    b = NSBatch([spec])
+    st = b.run(block=4)
+    om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    o = oracle_mod.ns_run(om, key, n, 4 * D, max_samples=spec.max_samples, term_cond={"peak_XL_frac": 0.01})
+    assert int(st["termination_reason"][0]) & 2048
+    assert int(o.termination_reason) & 2048
+    assert abs(int(st["iterations"][0]) - int(o.iterations)) <= 1
