@@ -217,7 +217,7 @@ def main():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--only-dim", type=int, default=None,
                     help="config3: keep only runs of this dimension (repeated to --runs); for kernel profiling")
-    ap.add_argument("--plain-problems", type=int, default=4,
+    ap.add_argument("--plain-problems", type=int, default=3,
                     help="blr workloads: problems in the plain GPU + finite-difference comparison")
     ap.add_argument("--no-e2e", action="store_true",
                     help="blr workloads: skip the end-to-end pass (one more full step)")
@@ -681,11 +681,14 @@ def main_blr(args):
         # plain GPU path + finite differences: problems one at a time, eager launches, five
         # runs each (theta, log tau +- h, log sigma +- h), no adjoint
         h = 1e-3
-        # the plain path takes ~5x the batched work one problem at a time, so it is sampled on
-        # the cheapest problems (by evaluations x N x P): its problems/s is then an upper
-        # bound and the fused speed-up a lower bound
-        cost = evals * Ns * Ps
-        idx = sorted(np.argsort(cost)[:min(args.plain_problems, R)].tolist())
+        # the plain path runs each problem five times, one problem at a time, so it is timed on
+        # problems at evenly spaced quantiles of the lock-step steps each problem needed in the
+        # fused run (evaluations / chains), and its time for the whole batch is estimated as
+        # (plain seconds per step of the sample) x (the batch's total steps)
+        steps = evals / np.array([s.shell_size for s in b.specs], np.float64)
+        order = np.argsort(steps)
+        K = min(args.plain_problems, R)
+        idx = sorted({int(order[int(round((q + 1) * R / (K + 1))) - 1]) for q in range(K)}) if R > 1 else [0]
         tot, fd = 0.0, []
         for r in idx:
             lz = []
@@ -701,9 +704,12 @@ def main_blr(args):
                 del one
             fd.append([(lz[1] - lz[2]) / (2 * h), (lz[3] - lz[4]) / (2 * h)])
         fd = np.array(fd)
-        plain = len(idx) / tot
-        line["plain_gpu_plus_fd"] = {"problems_per_s": plain, "sample": f"problems {idx} (the cheapest by evaluations x "
-                                     "N x P), 5 eager single-problem runs each", "fused_speedup": value / world / plain,
+        plain_total = tot / float(np.sum(steps[idx])) * float(np.sum(steps))
+        plain = R / plain_total
+        line["plain_gpu_plus_fd"] = {"problems_per_s": plain, "sample": f"problems {idx} at evenly spaced quantiles of "
+                                     "the lock-step steps per problem, 5 eager single-problem runs each "
+                                     f"({tot:.1f} s); batch time estimated as seconds per step of the sample x the "
+                                     f"batch's total steps ({plain_total:.1f} s)", "fused_speedup": value / world / plain,
                                      "fd_grad_rel_err_median": [float(v) for v in np.median(
                                          np.abs(fd - g_true[idx]) / np.abs(g_true[idx]), 0)]}
     if rank == 0 and not args.no_cpu:

@@ -422,6 +422,12 @@ __device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ 
 
 // ------------------------------------------------------------- likelihood ----
 
+// Programmatic dependent launch: let the next kernel in the stream start its prologue, and
+// wait for the previous kernel's grid (and its memory) before reading what it wrote.  Both are
+// no-ops for a kernel launched without the programmatic-serialisation attribute.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait_prior_grid() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
 // x = hi + lo with hi and lo both TF32 (round to nearest, ties away): the operand split of
 // the 3xTF32 tensor-core contraction (hi*hi + hi*lo + lo*hi).
 __device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {

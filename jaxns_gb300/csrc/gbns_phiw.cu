@@ -119,6 +119,8 @@ __global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
 // proposal w or finish the chain.  One warp per chain, lanes over the dimensions
 // (p = lane, lane + 32), so every per-dimension read and write is a coalesced row access.
 __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains) {
+  pdl_launch_dependents();
+  pdl_wait_prior_grid();  // the residuals of the previous step
   const long long g = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (g >= total_chains) return;
@@ -443,9 +445,19 @@ cudaError_t launch_lg_begin(const gbns_batch &b, const gbns_lg_bufs &lg, long lo
 }
 
 cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
-  if (lg.total_chains > 0)  // 8 chains (warps) per CTA
-    k_lg_step<<<(unsigned)((lg.total_chains + 7) / 8), 256, 0, s>>>(b, lg, lg.total_chains);
-  return cudaGetLastError();
+  if (lg.total_chains <= 0) return cudaSuccess;
+  // 8 chains (warps) per CTA; programmatic serialisation: may start while the previous
+  // residual launch drains (the kernel waits for it before reading)
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)((lg.total_chains + 7) / 8));
+  cfg.blockDim = dim3(256);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_lg_step, b, lg, (long long)lg.total_chains);
 }
 
 cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {

@@ -307,6 +307,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
   auto phi_lo = [&](int p, int kb) { return base + (uint32_t)(2 * NK + p * 2 * NK + NK + kb) * SR_BOX; };
   auto bar = [&](int q) { return smem_u32(&bars[q]); };
 
+  pdl_launch_dependents();
   if (tid == 0) {
     mbar_init(bar(0), 1);
     mbar_init(bar(1), 1);
@@ -332,6 +333,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
   const uint32_t tmem = tmem_slot;
   const volatile int *ab = &abort_flag;
   const int nunits = lg.num_items_tc;
+  pdl_wait_prior_grid();  // the chain step's proposals and tile marks
 
   if (warp == 0) {
     // ---- producer: W tile per unit, Phi hi / lo per row tile (two stages)
@@ -651,7 +653,21 @@ cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int 
   const int launches = steps < 0 ? 1 : steps;
   for (int q = 0; q < launches; ++q) {
     if (steps >= 0 && (e = launch_lg_step_kernel(b, lg, s)) != cudaSuccess) return e;
-    if (grid > 0) k_lg_resid_tc<<<grid, SR_THREADS, smem, s>>>(maps, b, lg, nkb, acc_stages);
+    if (grid > 0) {
+      // programmatic serialisation: the prologue (barriers, tensor memory) overlaps the chain
+      // step's tail; the kernel waits for that grid before reading its output
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3((unsigned)grid);
+      cfg.blockDim = dim3(SR_THREADS);
+      cfg.dynamicSmemBytes = smem;
+      cfg.stream = s;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+      attr[0].val.programmaticStreamSerializationAllowed = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      if ((e = cudaLaunchKernelEx(&cfg, k_lg_resid_tc, maps, b, lg, nkb, acc_stages)) != cudaSuccess) return e;
+    }
   }
   return cudaGetLastError();
 }
