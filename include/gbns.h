@@ -211,10 +211,7 @@ typedef struct {
     const int *tile_base;                   /* [R] first 128-chain tile of each run */
     int *tile_pending;                      /* [num_tiles] set by the chain step when a chain of the tile
                                                has a pending proposal; cleared by the residual launch */
-    int *tc_done;                           /* [groups] CTA completion counters of the residual launches (zeroed) */
-    int groups;                             /* 1..4 lock-step groups: chain tile t belongs to group t % groups;
-                                               the groups step on parallel streams (forked and joined with
-                                               events inside gbns_lg_steps); 1 on the CUDA-core path */
+    int *tc_done;                           /* [1] CTA completion counter of the residual launch (zeroed) */
 } gbns_lg_bufs;
 
 /* results buffers (device) */

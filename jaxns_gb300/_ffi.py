@@ -72,8 +72,7 @@ class LGBufs(ctypes.Structure):
                 ("use_tc", c_int), ("num_items_tc", c_int), ("items_tc", c_void_p), ("W_hi", c_void_p),
                 ("W_lo", c_void_p), ("Phi_hi", c_void_p), ("Phi_lo", c_void_p),
                 ("row_base", c_void_p), ("total_rows", c_ll), ("num_ctas_tc", c_int), ("num_tiles", c_int),
-                ("chain_run", c_void_p), ("tile_base", c_void_p), ("tile_pending", c_void_p), ("tc_done", c_void_p),
-                ("groups", c_int)]
+                ("chain_run", c_void_p), ("tile_base", c_void_p), ("tile_pending", c_void_p), ("tc_done", c_void_p)]
 
 
 class ResultsBufs(ctypes.Structure):

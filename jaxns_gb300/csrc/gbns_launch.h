@@ -20,7 +20,7 @@ cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long l
 cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream);
 cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
-cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream, int group);
+cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t stream);
 cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_adjoint_reduce(const double *log_w, long long M, int N, double log_sigma, const double *ss,

@@ -118,8 +118,7 @@ __global__ void k_lg_init(gbns_batch b, gbns_lg_bufs lg, long long total_chains)
 // One likelihood evaluation per chain: consume the pending result, then prepare the next
 // proposal w or finish the chain.  One warp per chain, lanes over the dimensions
 // (p = lane, lane + 32), so every per-dimension read and write is a coalesced row access.
-// group >= 0: only the chains of 128-chain tiles t with t % lg.groups == group.
-__global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains, int group) {
+__global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, long long total_chains) {
   pdl_launch_dependents();
   pdl_wait_prior_grid();  // the residuals of the previous step
   const long long g = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
@@ -131,7 +130,6 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
   if (rd.family != GBNS_LIK_LINGAUSS || st.done || st.phase != 1) return;
   const int c = (int)(g - rd.shell_off);
   if (c >= rd.s) return;
-  if (group >= 0 && (c >> 7) % lg.groups != group) return;
   int flags = lg.flags[g];
   if (flags & LG_DONE) return;
   const int P = rd.D, S = rd.S, K = rd.K, N = rd.N;
@@ -446,7 +444,7 @@ cudaError_t launch_lg_begin(const gbns_batch &b, const gbns_lg_bufs &lg, long lo
   return cudaGetLastError();
 }
 
-cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s, int group) {
+cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
   if (lg.total_chains <= 0) return cudaSuccess;
   // 8 chains (warps) per CTA; programmatic serialisation: may start while the previous
   // residual launch drains (the kernel waits for it before reading)
@@ -459,7 +457,7 @@ cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, c
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_lg_step, b, lg, (long long)lg.total_chains, group);
+  return cudaLaunchKernelEx(&cfg, k_lg_step, b, lg, (long long)lg.total_chains);
 }
 
 cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
@@ -472,9 +470,8 @@ cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cuda
 
 cudaError_t launch_lg_steps(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t s) {
   if (lg.use_tc) return launch_lg_steps_tc(b, lg, steps, s);
-  // CUDA-core residual: one group
   for (int q = 0; q < steps; ++q) {
-    cudaError_t e = launch_lg_step_kernel(b, lg, s, -1);
+    cudaError_t e = launch_lg_step_kernel(b, lg, s);
     if (e == cudaSuccess) e = launch_lg_resid_cc(b, lg, s);
     if (e != cudaSuccess) return e;
   }
@@ -515,8 +512,7 @@ int lg_check(const gbns_batch *batch, const gbns_lg_bufs *lg) {
     return lg_fail(-1, "gbns_lg: bad arguments (1 <= pmax <= 64, chain buffers required)");
   if (lg->use_tc && (!lg->W_hi || !lg->W_lo || !lg->Phi_hi || !lg->Phi_lo || !lg->row_base || lg->total_rows < 1 ||
                      lg->num_items_tc < 0 || lg->num_ctas_tc < 0 || (lg->num_items_tc > 0 && !lg->items_tc) ||
-                     !lg->tile_base || !lg->tile_pending || !lg->tc_done || lg->num_tiles < 0 || lg->groups < 1 ||
-                     lg->groups > 4))
+                     !lg->tile_base || !lg->tile_pending || !lg->tc_done || lg->num_tiles < 0))
     return lg_fail(-1, "gbns_lg: use_tc needs W_hi, W_lo, Phi_hi, Phi_lo, row_base, items_tc and num_ctas_tc >= 0");
   return 0;
 }
@@ -546,9 +542,7 @@ int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps
 int gbns_lg_chain_step(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
   int rc = lg_check(batch, lg);
   if (rc) return rc;
-  cudaError_t e = cudaSuccess;
-  for (int g = 0; g < (lg->use_tc ? lg->groups : 1) && e == cudaSuccess; ++g)
-    e = gbns::launch_lg_step_kernel(*batch, *lg, (cudaStream_t)stream, lg->use_tc ? g : -1);
+  cudaError_t e = gbns::launch_lg_step_kernel(*batch, *lg, (cudaStream_t)stream);
   if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
   return 0;
 }

@@ -276,25 +276,22 @@ __device__ __forceinline__ bool mbar_wait_or_abort(uint32_t bar, uint32_t parity
   }
 }
 
-// Work unit u: false if it belongs to another lock-step group, the run is inactive or the
-// chain tile has no pending proposal (the chain step marks such tiles; every warp reaches the
-// same answer).
-__device__ __forceinline__ bool sr_unit(const gbns_batch &b, const gbns_lg_bufs &lg, int u, int lane, int group,
-                                        int &r, int &c0, int &rt0, int &nrt) {
+// Work unit u: false if the run is inactive or the chain tile has no pending proposal (the
+// chain step marks such tiles; every warp reaches the same answer).
+__device__ __forceinline__ bool sr_unit(const gbns_batch &b, const gbns_lg_bufs &lg, int u, int lane, int &r, int &c0,
+                                        int &rt0, int &nrt) {
   const int *it = lg.items_tc + 4 * (size_t)u;
   r = it[0];
   c0 = it[1];
   rt0 = it[2];
   nrt = it[3];
-  if ((c0 >> 7) % lg.groups != group) return false;
   const gbns_run_state &st = b.state[r];
   if (st.done || st.phase != 1) return false;
   return __shfl_sync(0xffffffffu, lg.tile_pending[lg.tile_base[r] + (c0 >> 7)], 0) != 0;
 }
 
 __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constant__ SrMaps maps, gbns_batch b,
-                                                            gbns_lg_bufs lg, int nkb_max, int acc_stages,
-                                                            int group) {
+                                                            gbns_lg_bufs lg, int nkb_max, int acc_stages) {
   extern __shared__ unsigned char sr_dyn[];
   // 0 w_full, 1 w_empty, 2-3 phi_full, 4-5 phi_empty, 6-9 acc_full, 10-13 acc_empty
   __shared__ __align__(8) unsigned long long bars[14];
@@ -343,7 +340,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
     int wuse = 0, pt = 0;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
       int r, c0, rt0, nrt;
-      if (!sr_unit(b, lg, u, lane, group, r, c0, rt0, nrt)) continue;
+      if (!sr_unit(b, lg, u, lane, r, c0, rt0, nrt)) continue;
       const gbns_run_desc &rd = b.runs[r];
       const int nkb = (rd.D + TC_KB - 1) / TC_KB;
       const int brow = (int)lg.row_base[r];
@@ -393,7 +390,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
     int wuse = 0, pt = 0, at = 0;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
       int r, c0, rt0, nrt;
-      if (!sr_unit(b, lg, u, lane, group, r, c0, rt0, nrt)) continue;
+      if (!sr_unit(b, lg, u, lane, r, c0, rt0, nrt)) continue;
       const gbns_run_desc &rd = b.runs[r];
       const int nk8 = (rd.D + 7) / 8;
       int failed = 0;
@@ -437,7 +434,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
     int at = 0;
     for (int u = blockIdx.x; u < nunits; u += gridDim.x) {
       int r, c0, rt0, nrt;
-      if (!sr_unit(b, lg, u, lane, group, r, c0, rt0, nrt)) continue;
+      if (!sr_unit(b, lg, u, lane, r, c0, rt0, nrt)) continue;
       const gbns_run_desc &rd = b.runs[r];
       const int N = rd.N;
       const float *y = b.fparams + rd.param_off + (size_t)N * rd.D;
@@ -505,20 +502,16 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
                  "r"((uint32_t)(acc_stages * SR_ROWS))
                  : "memory");
   }
-  // the last CTA to finish clears its group's pending-tile marks for the next chain step
+  // the last CTA to finish clears the pending-tile marks for the next chain step
   __shared__ int last;
   if (tid == 0) {
     __threadfence();
-    last = atomicAdd(&lg.tc_done[group], 1) == (int)gridDim.x - 1;
+    last = atomicAdd(lg.tc_done, 1) == (int)gridDim.x - 1;
   }
   __syncthreads();
   if (last) {
-    for (int r = 0; r < b.num_runs; ++r) {
-      const int t0 = lg.tile_base[r], t1 = r + 1 < b.num_runs ? lg.tile_base[r + 1] : lg.num_tiles;
-      for (int t = t0 + tid; t < t1; t += blockDim.x)
-        if ((t - t0) % lg.groups == group) lg.tile_pending[t] = 0;
-    }
-    if (tid == 0) lg.tc_done[group] = 0;
+    for (int q = tid; q < lg.num_tiles; q += blockDim.x) lg.tile_pending[q] = 0;
+    if (tid == 0) *lg.tc_done = 0;
   }
 }
 
@@ -625,41 +618,11 @@ cudaError_t set_smem_attrs() {
   return err;
 }
 
-// Auxiliary streams and fork / join events of the lock-step groups, one set per device,
-// created outside any stream capture (by gbns_lg_prepare_tc).
-struct GroupStreams {
-  cudaStream_t aux[3];
-  cudaEvent_t fork, join[3];
-  bool ready;
-};
-GroupStreams g_groups[64];
-std::mutex g_groups_mu;
-
-cudaError_t group_streams(GroupStreams **out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  std::lock_guard<std::mutex> lock(g_groups_mu);
-  GroupStreams &gs = g_groups[dev];
-  if (!gs.ready) {
-    for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaStreamCreateWithFlags(&gs.aux[q], cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&gs.fork, cudaEventDisableTiming);
-    for (int q = 0; q < 3 && e == cudaSuccess; ++q) e = cudaEventCreateWithFlags(&gs.join[q], cudaEventDisableTiming);
-    if (e != cudaSuccess) return e;
-    gs.ready = true;
-  }
-  *out = &gs;
-  return cudaSuccess;
-}
-
 }  // namespace
 
 cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
   cudaError_t e = set_smem_attrs();
   if (e != cudaSuccess) return e;
-  GroupStreams *gs = nullptr;
-  if (lg.groups > 1 && (e = group_streams(&gs)) != cudaSuccess) return e;
   const long long n = lg.total_rows * 64;
   if (n > 0) k_split_phi<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(b, lg);
   return cudaGetLastError();
@@ -684,43 +647,26 @@ cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int 
   int dev = 0, sms = 0;
   if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
   if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  const int G = lg.groups;
-  int grid = (sms * per_sm + G - 1) / G;  // the groups share the SMs
+  int grid = sms * per_sm;
   if (lg.num_ctas_tc > 0 && lg.num_ctas_tc < grid) grid = lg.num_ctas_tc;
-  if (grid > (lg.num_items_tc + G - 1) / G) grid = (lg.num_items_tc + G - 1) / G;
+  if (grid > lg.num_items_tc) grid = lg.num_items_tc;
   const int launches = steps < 0 ? 1 : steps;
-  // groups > 1: group g steps on its own stream, forked from s and joined back into it
-  GroupStreams *gs = nullptr;
-  if (G > 1 && steps >= 0) {
-    if ((e = group_streams(&gs)) != cudaSuccess) return e;
-    if ((e = cudaEventRecord(gs->fork, s)) != cudaSuccess) return e;
-    for (int g = 1; g < G; ++g)
-      if ((e = cudaStreamWaitEvent(gs->aux[g - 1], gs->fork, 0)) != cudaSuccess) return e;
-  }
-  for (int g = 0; g < G; ++g) {
-    const cudaStream_t sg = (gs && g > 0) ? gs->aux[g - 1] : s;
-    for (int q = 0; q < launches; ++q) {
-      if (steps >= 0 && (e = launch_lg_step_kernel(b, lg, sg, g)) != cudaSuccess) return e;
-      if (grid <= 0) continue;
+  for (int q = 0; q < launches; ++q) {
+    if (steps >= 0 && (e = launch_lg_step_kernel(b, lg, s)) != cudaSuccess) return e;
+    if (grid > 0) {
       // programmatic serialisation: the prologue (barriers, tensor memory) overlaps the chain
       // step's tail; the kernel waits for that grid before reading its output
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3((unsigned)grid);
       cfg.blockDim = dim3(SR_THREADS);
       cfg.dynamicSmemBytes = smem;
-      cfg.stream = sg;
+      cfg.stream = s;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
       attr[0].val.programmaticStreamSerializationAllowed = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      if ((e = cudaLaunchKernelEx(&cfg, k_lg_resid_tc, maps, b, lg, nkb, acc_stages, g)) != cudaSuccess) return e;
-    }
-  }
-  if (gs) {
-    for (int g = 1; g < G; ++g) {
-      if ((e = cudaEventRecord(gs->join[g - 1], gs->aux[g - 1])) != cudaSuccess) return e;
-      if ((e = cudaStreamWaitEvent(s, gs->join[g - 1], 0)) != cudaSuccess) return e;
+      if ((e = cudaLaunchKernelEx(&cfg, k_lg_resid_tc, maps, b, lg, nkb, acc_stages)) != cudaSuccess) return e;
     }
   }
   return cudaGetLastError();

@@ -300,7 +300,6 @@ class NSBatch:
         g.total_chains = nc
         if g.pmax > 64:
             raise ValueError("the linear-Gaussian path supports P <= 64")
-        g.groups = 1
         self.lg_tc = bool(tensor_cores)
         if self.lg_tc:
             Ns = np.array([s.N for s in specs], np.int64)
@@ -319,13 +318,10 @@ class NSBatch:
                                 items_tc=torch.tensor(np.array(items_tc, np.int32).reshape(-1, 4), device=dev))
             tile_base = np.concatenate([[0], np.cumsum([ct for ct, _ in tiles])[:-1]]).astype(np.int32)
             self.lg_tc_t.update(tile_base=torch.tensor(tile_base, device=dev),
-                                tile_pending=z(sum(ct for ct, _ in tiles), torch.int32), tc_done=z(4, torch.int32))
+                                tile_pending=z(sum(ct for ct, _ in tiles), torch.int32), tc_done=z(1, torch.int32))
             for k, v in self.lg_tc_t.items():
                 setattr(g, k, v.data_ptr())
             g.num_tiles = int(sum(ct for ct, _ in tiles))
-            # small batches (fewer work units than about two per SM) step in two groups of
-            # chain tiles on parallel streams, so two latency-bound lock steps share the GPU
-            g.groups = 2 if (g.num_tiles >= 2 and len(items_tc) <= 2 * 152) else 1
             g.num_items_tc = len(items_tc)
             g.total_rows = rows
             g.use_tc = 1
