@@ -75,12 +75,13 @@ __device__ __forceinline__ float slice_alpha(int j, int S) {
   return 0.5f * (1.0f - step) + step;
 }
 
-// Minimum resident CTAs per SM (caps registers at 64 for 8): the sampler is latency-bound, and
+// Minimum resident CTAs per SM (8 caps registers at 64): the sampler is latency-bound, and
 // at DMAX <= 8 the cap costs at most 8 B of spills per thread; Gaussian shells at DMAX 16 runs
 // 4.8 % faster capped (172 B of spills) than at its natural 112 registers (4 CTAs per SM).
+// The other instantiations keep the occupancy they reach without a cap (3 or 4 CTAs).
 template <int DMAX, int FAM>
 constexpr int slice_min_blocks() {
-  return (DMAX <= 8 || (DMAX == 16 && FAM == GBNS_LIK_SHELLS)) ? 8 : 1;
+  return (DMAX <= 8 || (DMAX == 16 && FAM == GBNS_LIK_SHELLS)) ? 8 : (DMAX >= 64 ? 3 : 4);
 }
 
 template <int DMAX, int FAM>
