@@ -171,6 +171,10 @@ typedef struct {
     int bucket_end[8];
     int chains_per_item;
     int max_evals_per_slice;        /* shrink-loop evaluation budget per slice */
+    int gradient_guided;            /* UniDimSliceSampler(gradient_guided=True): after each accepted point
+                                       the direction is reflected about the U-space gradient of log L
+                                       (thread-per-chain sampler: MVN D <= 16 and shells) */
+    int pad_gg;
 } gbns_batch;
 
 /* Lock-step chain state of the linear-Gaussian family (device, caller-allocated).  Its

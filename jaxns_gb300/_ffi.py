@@ -60,7 +60,8 @@ class Batch(ctypes.Structure):
                 ("store_P", c_void_p), ("store_U", c_void_p), ("fparams", c_void_p), ("prior_kind", c_void_p),
                 ("prior_a", c_void_p), ("prior_b", c_void_p), ("ncoef", c_void_p), ("items", c_void_p),
                 ("num_items", c_int), ("bucket_begin", c_int * 8), ("bucket_end", c_int * 8),
-                ("chains_per_item", c_int), ("max_evals_per_slice", c_int)]
+                ("chains_per_item", c_int), ("max_evals_per_slice", c_int), ("gradient_guided", c_int),
+                ("pad_gg", c_int)]
 
 
 class LGBufs(ctypes.Structure):

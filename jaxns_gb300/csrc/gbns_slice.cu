@@ -23,6 +23,65 @@ struct RunSmem {
   int m;                                // live points above the contour
 };
 
+// jax.grad of Model.forward w.r.t. U at u (analytic): d log L / dx through the prior quantile
+// (Uniform: dx/du = b; Normal: dx/du = b sqrt(2 pi) exp(z^2 / 2)).  MVN: -Linv^T Linv (x - mu);
+// shells: sum_k softmax_k (-z_k / w) (x - c_k) / r_k.
+template <int DMAX, int FAM>
+__device__ __forceinline__ void grad_u(const RunSmem<DMAX, FAM> &P, int D, const float *u, float *g) {
+  float x[DMAX], dxdu[DMAX];
+#pragma unroll
+  for (int j = 0; j < DMAX; ++j) {
+    if (j < D) {
+      if (P.kind[j] == GBNS_PRIOR_UNIFORM) {
+        x[j] = fmaf(P.b[j], u[j], P.a[j]);
+        dxdu[j] = P.b[j];
+      } else {
+        const float z = GBNS_SQRT2F * erfinvf(fmaf(2.0f, u[j], -1.0f));
+        x[j] = fmaf(P.b[j], z, P.a[j]);
+        dxdu[j] = P.b[j] * 2.5066282746310002f * __expf(0.5f * z * z);
+      }
+    }
+  }
+  if (FAM == GBNS_LIK_MVN) {
+    float e[DMAX], z[DMAX];
+#pragma unroll
+    for (int j = 0; j < DMAX; ++j) e[j] = j < D ? x[j] - P.p0[j] : 0.0f;
+#pragma unroll
+    for (int i = 0; i < DMAX; ++i) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int j = 0; j <= i; ++j) acc = fmaf(P.p1[i * DMAX + j], e[j], acc);
+      z[i] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < DMAX; ++q) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int i = q; i < DMAX; ++i) acc = fmaf(P.p1[i * DMAX + q], z[i], acc);
+      if (q < D) g[q] = -acc * dxdu[q];
+    }
+  } else {
+    float r1 = 0.f, r2 = 0.f;
+#pragma unroll
+    for (int j = 0; j < DMAX; ++j) {
+      if (j < D) {
+        const float e1 = x[j] - P.p0[j], e2 = x[j] - P.p1[j];
+        r1 = fmaf(e1, e1, r1);
+        r2 = fmaf(e2, e2, r2);
+      }
+    }
+    r1 = sqrtf(r1);
+    r2 = sqrtf(r2);
+    const float z1 = (r1 - P.R) / P.w, z2 = (r2 - P.R) / P.w;
+    const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2, mx = fmaxf(s1, s2);
+    const float q1 = __expf(s1 - mx), q2 = __expf(s2 - mx), tot = q1 + q2;
+    const float f1 = (q1 / tot) * (-z1 / P.w) / r1, f2 = (q2 / tot) * (-z2 / P.w) / r2;
+#pragma unroll
+    for (int j = 0; j < DMAX; ++j)
+      if (j < D) g[j] = (f1 * (x[j] - P.p0[j]) + f2 * (x[j] - P.p1[j])) * dxdu[j];
+  }
+}
+
 template <int DMAX, int FAM>
 __device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, const float *u0, const float *d, float t) {
   float x[DMAX];
@@ -84,7 +143,9 @@ constexpr int slice_min_blocks() {
   return (DMAX <= 8 || (DMAX == 16 && FAM == GBNS_LIK_SHELLS)) ? 8 : (DMAX >= 64 ? 3 : 4);
 }
 
-template <int DMAX, int FAM>
+// GRAD: the gradient-guided variant (the direction of slice j + 1 is the reflection of slice
+// j's direction about the U-space gradient at the accepted point).
+template <int DMAX, int FAM, bool GRAD>
 __global__ void __launch_bounds__(128, slice_min_blocks<DMAX, FAM>()) k_slice_shell(gbns_batch b, int item_begin,
                                                                                  const float *__restrict__ Lstar_in,
                                                       const uint32_t *__restrict__ keys_in) {
@@ -282,7 +343,41 @@ __global__ void __launch_bounds__(128, slice_min_blocks<DMAX, FAM>()) k_slice_sh
       }
       ++j;
       start = true;
-      if (j < S) {
+      if (GRAD) {
+        // Householder reflection at the accepted point (uni_slice_sampler.py:255-269); a
+        // random direction from split(after_key)[0] when the gradient vanishes or is not
+        // finite.  The gradient counts as one likelihood evaluation, also after the last slice.
+        ++total;
+        if (j < S) {
+          float g[DMAX];
+          grad_u<DMAX, FAM>(P, D, u0, g);
+          float gg = 0.0f;
+#pragma unroll
+          for (int q = 0; q < DMAX; ++q)
+            if (q < D) gg = fmaf(g[q], g[q], gg);
+          const float gn = sqrtf(gg);
+          if (!(gn >= 1e-10f) || isinf(gn)) {
+            need_dir = true;
+            dir_key = fold(after_key, 0u);
+          } else {
+            float dot = 0.0f;
+#pragma unroll
+            for (int q = 0; q < DMAX; ++q)
+              if (q < D) dot = fmaf(d[q], g[q] / gn, dot);
+            float dd = 0.0f;
+#pragma unroll
+            for (int q = 0; q < DMAX; ++q)
+              if (q < D) {
+                d[q] = fmaf(-2.0f * dot, g[q] / gn, d[q]);
+                dd = fmaf(d[q], d[q], dd);
+              }
+            const float dn = sqrtf(dd);
+#pragma unroll
+            for (int q = 0; q < DMAX; ++q)
+              if (q < D) d[q] = d[q] / dn;
+          }
+        }
+      } else if (j < S) {
         need_dir = true;
         dir_key = after_key;
       }
@@ -304,10 +399,15 @@ static cudaError_t launch_bucket(const gbns_batch &b, int fam, int ib, int ie, c
   const int nblk = ie - ib;
   if (nblk <= 0) return cudaSuccess;
   const int threads = b.chains_per_item;
+  constexpr int DM = DMAX <= 16 ? DMAX : 16;
   if (fam == GBNS_LIK_MVN) {
-    if (DMAX <= 16) k_slice_shell<(DMAX <= 16 ? DMAX : 16), GBNS_LIK_MVN><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+    if (DMAX <= 16) {
+      if (b.gradient_guided) k_slice_shell<DM, GBNS_LIK_MVN, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+      else k_slice_shell<DM, GBNS_LIK_MVN, false><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+    }
   } else {
-    k_slice_shell<DMAX, GBNS_LIK_SHELLS><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+    if (b.gradient_guided) k_slice_shell<DMAX, GBNS_LIK_SHELLS, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+    else k_slice_shell<DMAX, GBNS_LIK_SHELLS, false><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
   }
   return cudaGetLastError();
 }

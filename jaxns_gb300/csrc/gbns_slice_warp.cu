@@ -358,6 +358,9 @@ static cudaError_t launch_warp_bucket(const gbns_batch &b, int ib, int ie, const
 // MVN buckets 2 (16 < D <= 32) and 3 (32 < D <= 64) run here.
 cudaError_t launch_slice_warp(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream) {
   cudaError_t e;
+  // the gradient-guided slice runs on the thread-per-chain kernel only (MVN D <= 16)
+  if (b.gradient_guided && (b.bucket_end[2] > b.bucket_begin[2] || b.bucket_end[3] > b.bucket_begin[3]))
+    return cudaErrorNotSupported;
   if ((e = launch_warp_bucket<32>(b, b.bucket_begin[2], b.bucket_end[2], Lstar, keys, stream))) return e;
   if ((e = launch_warp_bucket<64>(b, b.bucket_begin[3], b.bucket_end[3], Lstar, keys, stream))) return e;
   return cudaSuccess;

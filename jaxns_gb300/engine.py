@@ -63,6 +63,7 @@ class RunSpec:
     store_U: bool = True
     N: int = 0
     log_L_offset: float = 0.0  # FP64 constant part of log L (device values are relative to it)
+    gradient_guided: bool = False
 
 
 def ncoef_table(nmax: int) -> np.ndarray:
@@ -139,6 +140,14 @@ class NSBatch:
         self.lg = FAMILY_LINGAUSS in fams
         if self.lg and len(fams) > 1:
             raise ValueError("a batch holds either linear-Gaussian runs only or none")
+        gg = {bool(s.gradient_guided) for s in specs}
+        if len(gg) > 1:
+            raise ValueError("a batch holds either gradient-guided runs only or none")
+        self.gradient_guided = gg.pop()
+        if self.gradient_guided and any(s.family == FAMILY_LINGAUSS or (s.family == FAMILY_MVN and s.D > 16)
+                                        for s in specs):
+            raise NotImplementedError("the gradient-guided slice runs on the thread-per-chain sampler: "
+                                      "correlated Gaussians with D <= 16 and Gaussian shells")
         for s in specs:
             _dbucket(s.D)
         live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])
@@ -259,6 +268,7 @@ class NSBatch:
             b.bucket_begin[k], b.bucket_end[k] = int(bb[k]), int(be[k])
         b.chains_per_item = CH
         b.max_evals_per_slice = int(max_evals_per_slice)
+        b.gradient_guided = int(self.gradient_guided)
         self._b = b
         self._lgb = self._alloc_lg(specs, ss, Ds, shell_off, lg_tensor_cores) if self.lg else None
         self._graphs: Dict[tuple, tuple] = {}

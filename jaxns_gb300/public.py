@@ -143,8 +143,8 @@ class UniDimSliceSampler:
             raise NotImplementedError("Adaptive shrinkage not implemented.")
         if not self.perfect:
             raise ValueError("Only perfect slice sampler is implemented.")
-        if self.gradient_slice or self.gradient_guided:
-            raise NotImplementedError("gradient-based slicing is not on the fused GPU path")
+        if self.gradient_slice:
+            raise NotImplementedError("gradient_slice (climb the gradient) is not on the fused GPU path")
 
     def num_phantom(self) -> int:
         return self.num_phantom_save
@@ -202,7 +202,8 @@ class ShardedStaticNestedSampler:
                        num_phantom=self.sampler.num_phantom(), midpoint_shrink=self.sampler.midpoint_shrink,
                        init_efficiency_threshold=self.init_efficiency_threshold, store_U=self.store_U,
                        N=int(getattr(m.log_likelihood, "Phi", np.zeros((0, 0))).shape[0]),
-                       log_L_offset=m.log_likelihood.log_L_offset())
+                       log_L_offset=m.log_likelihood.log_L_offset(),
+                       gradient_guided=bool(getattr(self.sampler, "gradient_guided", False)))
 
     def _run(self, key, term_cond: TerminationCondition):
         batch = NSBatch([self.run_spec(key, term_cond)], device="cuda")

@@ -203,6 +203,67 @@ void orc_forward_batch(const orc_model *m, const double *U, long B, double *out)
     for (long b = 0; b < B; ++b) out[b] = orc_forward(m, U + b * m->D);
 }
 
+/* jax.grad of Model.forward w.r.t. U, analytically: d log L / dX through the prior quantile
+ * (Uniform: dX/dU = high - low; Normal: dX/dU = scale sqrt(2 pi) exp(z^2 / 2), z the standard
+ * normal quantile of U). */
+void orc_grad_U(const orc_model *m, const double *U, double *g) {
+    int D = m->D;
+    double X[128], gx[128];
+    prior_transform(m, U, X);
+    if (m->family == ORC_LIK_MVN) {
+        const double *mu = m->p, *L = m->p + D;
+        double z[128];
+        for (int i = 0; i < D; ++i) {              /* L z = X - mu */
+            double acc = X[i] - mu[i];
+            for (int j = 0; j < i; ++j) acc -= L[i * D + j] * z[j];
+            z[i] = acc / L[i * D + i];
+        }
+        for (int i = D - 1; i >= 0; --i) {         /* L^T v = z, d log L / dX = -v */
+            double acc = z[i];
+            for (int j = i + 1; j < D; ++j) acc -= L[j * D + i] * gx[j];
+            gx[i] = acc / L[i * D + i];
+        }
+        for (int i = 0; i < D; ++i) gx[i] = -gx[i];
+    } else if (m->family == ORC_LIK_SHELLS) {
+        const double *c1 = m->p, *c2 = m->p + D;
+        double R = m->p[2 * D], w = m->p[2 * D + 1];
+        double r1 = 0, r2 = 0;
+        for (int j = 0; j < D; ++j) {
+            r1 += (X[j] - c1[j]) * (X[j] - c1[j]);
+            r2 += (X[j] - c2[j]) * (X[j] - c2[j]);
+        }
+        r1 = sqrt(r1);
+        r2 = sqrt(r2);
+        double z1 = (r1 - R) / w, z2 = (r2 - R) / w;
+        double s1 = -0.5 * z1 * z1, s2 = -0.5 * z2 * z2, mx = s1 > s2 ? s1 : s2;
+        double p1 = exp(s1 - mx), p2 = exp(s2 - mx), tot = p1 + p2;
+        p1 /= tot;
+        p2 /= tot;
+        for (int j = 0; j < D; ++j)
+            gx[j] = p1 * (-z1 / w) * (X[j] - c1[j]) / r1 + p2 * (-z2 / w) * (X[j] - c2[j]) / r2;
+    } else {
+        int N = m->N;
+        const double *Phi = m->p, *y = m->p + (size_t)N * D;
+        double sigma = m->p[(size_t)N * D + N];
+        for (int j = 0; j < D; ++j) gx[j] = 0.0;
+        for (int i = 0; i < N; ++i) {
+            double r = y[i];
+            for (int j = 0; j < D; ++j) r -= Phi[(size_t)i * D + j] * X[j];
+            for (int j = 0; j < D; ++j) gx[j] += Phi[(size_t)i * D + j] * r / (sigma * sigma);
+        }
+    }
+    for (int j = 0; j < D; ++j) {
+        double dxdu;
+        if (m->prior_kind[j] == ORC_PRIOR_UNIFORM) {
+            dxdu = m->prior_b[j];
+        } else {
+            double z = ORC_SQRT2 * orc_erfinv(2.0 * U[j] - 1.0);
+            dxdu = m->prior_b[j] * sqrt(2.0 * ORC_PI) * exp(0.5 * z * z);
+        }
+        g[j] = gx[j] * dxdu;
+    }
+}
+
 /* Model.sample_U (framework/model.py:135-138): uniform(split(key)[1], (D,)) via
  * Ctx.next_rng_key (framework/context.py:107-109). */
 static void sample_U(okey key, int D, double *U) {
@@ -249,6 +310,7 @@ typedef struct {
     int num_slices;
     int num_phantom;
     int midpoint_shrink;
+    int gradient_guided;
 } orc_slice_cfg;
 
 /* linspace(0.5, 1., S)[j] as jnp.linspace evaluates it. */
@@ -263,7 +325,7 @@ static double slice_alpha(int j, int S) {
  * U0/logL0 is the seed; on return U holds the accepted point, d the new direction. */
 static double new_proposal(const orc_model *m, okey key, const double *U0, double logL0,
                            double *d, int midpoint, double alpha, double Lstar, double *U,
-                           long *nevals) {
+                           long *nevals, int gradient_guided) {
     int D = m->D;
     okey run_key = key_fold(key, 0);
     okey t_key = key_fold(key, 2);
@@ -289,7 +351,26 @@ static double new_proposal(const orc_model *m, okey key, const double *U0, doubl
         ne += 1;
         ck = nk;
     }
-    sample_direction(after_key, D, d);
+    if (gradient_guided) {
+        /* Householder reflection of the direction at the accepted point
+         * (uni_slice_sampler.py:255-269); a random direction from split(after_key)[0] when the
+         * gradient vanishes or is not finite.  The gradient counts as one evaluation. */
+        double g[128], gn = 0.0, dot = 0.0, dn = 0.0;
+        orc_grad_U(m, U, g);
+        ne += 1;
+        for (int j = 0; j < D; ++j) gn += g[j] * g[j];
+        gn = sqrt(gn);
+        if (gn < 1e-10 || !isfinite(gn)) {
+            sample_direction(key_fold(after_key, 0), D, d);
+        } else {
+            for (int j = 0; j < D; ++j) { g[j] /= gn; dot += d[j] * g[j]; }
+            for (int j = 0; j < D; ++j) { d[j] -= 2.0 * dot * g[j]; dn += d[j] * d[j]; }
+            dn = sqrt(dn);
+            for (int j = 0; j < D; ++j) d[j] /= dn;
+        }
+    } else {
+        sample_direction(after_key, D, d);
+    }
     *nevals = ne;
     return logL;
 }
@@ -343,7 +424,7 @@ void orc_slice_get_sample(const orc_model *m, const orc_slice_cfg *cfg, uint32_t
         okey kj = key_fold(slices_key, (uint64_t)j);
         long ne;
         double logL = new_proposal(m, kj, U0, logL0, d, cfg->midpoint_shrink, slice_alpha(j, S), Lstar,
-                                   U, &ne);
+                                   U, &ne, cfg->gradient_guided);
         total += ne;
         memcpy(U0, U, sizeof(double) * D);
         logL0 = logL;

@@ -52,7 +52,7 @@ class _Model(ctypes.Structure):
 
 class _SliceCfg(ctypes.Structure):
     _fields_ = [("num_slices", ctypes.c_int), ("num_phantom", ctypes.c_int),
-                ("midpoint_shrink", ctypes.c_int)]
+                ("midpoint_shrink", ctypes.c_int), ("gradient_guided", ctypes.c_int)]
 
 
 class _NSCfg(ctypes.Structure):
@@ -236,12 +236,21 @@ def forward(model: OracleModel, U):
 
 # -------------------------------------------------------------------- samplers
 
+def grad_U(model, U):
+    """jax.grad of Model.forward w.r.t. U (analytic, FP64)."""
+    U = np.ascontiguousarray(U, np.float64)
+    g = np.zeros(model.D)
+    m = model._c()
+    lib().orc_grad_U(ctypes.byref(m), _dp(U), _dp(g))
+    return g
+
+
 def slice_get_sample(model, key, L_star, live_U, live_logL, num_slices, num_phantom=0,
-                     midpoint_shrink=True):
+                     midpoint_shrink=True, gradient_guided=False):
     D = model.D
     live_U = np.ascontiguousarray(live_U, np.float64)
     live_logL = np.ascontiguousarray(live_logL, np.float64)
-    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink))
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided))
     U = np.zeros(D)
     logL = ctypes.c_double()
     ne = ctypes.c_long()
@@ -256,11 +265,11 @@ def slice_get_sample(model, key, L_star, live_U, live_logL, num_slices, num_phan
 
 
 def slice_shell(model, key, L_star, live_U, live_logL, num_chains, num_slices, num_phantom=0,
-                midpoint_shrink=True):
+                midpoint_shrink=True, gradient_guided=False):
     D = model.D
     live_U = np.ascontiguousarray(live_U, np.float64)
     live_logL = np.ascontiguousarray(live_logL, np.float64)
-    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink))
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided))
     U = np.zeros((num_chains, D))
     L = np.zeros(num_chains)
     E = np.zeros(num_chains, np.int64)
@@ -425,7 +434,8 @@ def round_up_max_samples(max_samples, num_discard, num_phantom):
 
 def ns_run(model: OracleModel, key, num_live_points, num_slices, max_samples=None, num_phantom=0,
            midpoint_shrink=True, shell_fraction=0.5, init_efficiency_threshold=0.1,
-           term_cond: Optional[dict] = None, max_iterations=0, init_only=False) -> OracleRun:
+           term_cond: Optional[dict] = None, max_iterations=0, init_only=False,
+           gradient_guided=False) -> OracleRun:
     """NestedSampler(...)(key, term_cond) followed by to_results(trim=True)."""
     shell_fraction = max(shell_fraction, 1.0 / num_live_points)
     n = round_up_num_live_points(num_live_points, shell_fraction)
@@ -437,7 +447,8 @@ def ns_run(model: OracleModel, key, num_live_points, num_slices, max_samples=Non
     big = float(np.iinfo(np.int64).max)
     tc["max_samples"] = min(float(tc.get("max_samples") or big), float(cap))
     cfg = _NSCfg(n, s, cap, float(init_efficiency_threshold), _SliceCfg(num_slices, num_phantom,
-                                                                      int(midpoint_shrink)), 100)
+                                                                      int(midpoint_shrink),
+                                                                      int(gradient_guided)), 100)
     D = model.D
     sender = np.zeros(cap, np.int64)
     log_L = np.zeros(cap)
@@ -492,7 +503,7 @@ def ns_run_batch(models, cfg_list, keys, term_conds, num_threads, max_iterations
         n = c["num_live_points"]
         s = n // 2
         cap = round_up_max_samples(c["max_samples"], s, c.get("num_phantom", 0))
-        cs[r] = _NSCfg(n, s, cap, 0.1, _SliceCfg(c["num_slices"], c.get("num_phantom", 0), 1), 100)
+        cs[r] = _NSCfg(n, s, cap, 0.1, _SliceCfg(c["num_slices"], c.get("num_phantom", 0), 1, 0), 100)
         tc = dict(term_conds[r])
         tc["max_samples"] = min(float(tc.get("max_samples") or cap), float(cap))
         ts[r] = make_term_cond(**tc)

@@ -217,3 +217,24 @@ def test_oracle_reweighted_gradient_matches_fd(oracle_mod):
           (oracle_mod.blr_reweighted(Phi, y, U, log_w, lt, ls + h)[0] -
            oracle_mod.blr_reweighted(Phi, y, U, log_w, lt, ls - h)[0]) / (2 * h)]
     np.testing.assert_allclose(g, fd, rtol=1e-6, atol=1e-6)
+
+
+def test_grad_U_matches_finite_differences(oracle_mod):
+    """The oracle's analytic U-space gradients (used by the gradient-guided slice) against
+    central differences of its own forward, for MVN, shells and the linear-Gaussian family,
+    Uniform and Normal priors."""
+    rng = np.random.default_rng(0)
+    D = 4
+    A = rng.standard_normal((D, D))
+    models = [oracle_mod.mvn_model(-3 * np.ones(D), 3 * np.ones(D), rng.standard_normal(D), A @ A.T / D + 0.5 * np.eye(D)),
+              oracle_mod.shells_model(-2, 2, 0.4 * np.ones(D), -0.4 * np.ones(D), 0.8, 0.3)]
+    Phi = rng.standard_normal((30, D))
+    models.append(oracle_mod.lingauss_model(Phi, Phi @ rng.standard_normal(D), 0.7, 1.3))
+    for m in models:
+        for _ in range(3):
+            U = rng.uniform(0.2, 0.8, D)
+            g = oracle_mod.grad_U(m, U)
+            h = 1e-6
+            fd = np.array([(oracle_mod.forward(m, (U + h * e)[None])[0] - oracle_mod.forward(m, (U - h * e)[None])[0])
+                           / (2 * h) for e in np.eye(D)])
+            np.testing.assert_allclose(g, fd, rtol=1e-5, atol=1e-6 * max(1.0, np.abs(fd).max()))
