@@ -144,9 +144,10 @@ constexpr int slice_min_blocks() {
 }
 
 // GRAD: the gradient-guided variant (the direction of slice j + 1 is the reflection of slice
-// j's direction about the U-space gradient at the accepted point).
+// j's direction about the U-space gradient at the accepted point); it keeps its gradient
+// arrays in registers at 2 CTAs per SM instead of spilling them.
 template <int DMAX, int FAM, bool GRAD>
-__global__ void __launch_bounds__(128, slice_min_blocks<DMAX, FAM>()) k_slice_shell(gbns_batch b, int item_begin,
+__global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>()) k_slice_shell(gbns_batch b, int item_begin,
                                                                                  const float *__restrict__ Lstar_in,
                                                       const uint32_t *__restrict__ keys_in) {
   __shared__ RunSmem<DMAX, FAM> P;
