@@ -279,8 +279,9 @@ def main():
     from jaxns_gb300.batched import BatchedNestedSampler
     import jaxns_gb300 as gb
 
+    from jaxns_gb300.replicas import reduce_timing, replica_keys
     samplers = make_samplers(wl)
-    keys = np.array([gb.random.PRNGKey(r) for r in range(len(wl))])
+    keys = replica_keys(rank, len(wl))  # independent seeds on every rank
     bns = BatchedNestedSampler(samplers, keys, [gb.TerminationCondition(dlogZ=1e-4)] * len(wl), block=args.block)
     b = bns.batch
     if args.iterations is not None:
@@ -334,13 +335,11 @@ def main():
     ms = ev0.elapsed_time(ev1)
     gpu_launches = b.kernel_launches - launches0
     st = b.state()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    runs_total = args.runs * args.steps * world
+    # slowest rank's time, units of all ranks
+    ms, runs_total = reduce_timing(ms, args.runs * args.steps, device="cuda")
+    _, nevals_total = reduce_timing(0.0, nevals, device="cuda")
     value = runs_total / (ms / 1e3)
-    evals_per_s = nevals * world / (ms / 1e3)
+    evals_per_s = nevals_total / (ms / 1e3)
 
     # sampler-kernel roofline (FP32 CUDA-core bound): algorithmic flops / sampler device time
     Dr = np.array([w[0] for w in wl])
@@ -371,7 +370,7 @@ def main():
         sc = step(from_host=True)
     e1.record()
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
+    e2e_ms, _ = reduce_timing(e0.elapsed_time(e1), 0, device="cuda")
     e2e = {"value": runs_total / (e2e_ms / 1e3), "unit": "runs/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
@@ -531,9 +530,10 @@ def main_blr(args):
     from jaxns_gb300.batched import BatchedNestedSampler
     from jaxns_gb300.engine import NSBatch
 
+    from jaxns_gb300.replicas import reduce_timing, replica_keys
     wl = blr_workload(args.runs, 2024 + rank, name)
     R = len(wl)
-    keys = np.array([gb.random.PRNGKey(r) for r in range(R)])
+    keys = replica_keys(rank, R)
     bns = BatchedNestedSampler([blr_sampler(p) for p in wl], keys, None, store_U=not args.kernel_profile,
                                lg_tensor_cores=not args.cuda_core)
     b = bns.batch
@@ -586,11 +586,9 @@ def main_blr(args):
     ms = ev0.elapsed_time(ev1)
     gpu_launches = b.kernel_launches - launches0
     st = b.state()
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = R * args.steps * world / (ms / 1e3)
+    ms, problems_total = reduce_timing(ms, R * args.steps, device="cuda")
+    _, nevals = reduce_timing(0.0, nevals, device="cuda")
+    value = problems_total / (ms / 1e3)
     Ns = np.array([p["N"] for p in wl], np.float64)
     Ps = np.array([p["P"] for p in wl], np.float64)
     evals = st["num_likelihood_evaluations"].astype(np.float64)
@@ -662,8 +660,8 @@ def main_blr(args):
             host_out, h2d = step(from_host=True)
         e1_.record()
         barrier()
-        e2e_ms = e0_.elapsed_time(e1_)
-        e2e = {"value": R * args.steps * world / (e2e_ms / 1e3), "unit": "problems/s", "h2d_bytes_per_step": h2d,
+        e2e_ms, _ = reduce_timing(e0_.elapsed_time(e1_), 0, device="cuda")
+        e2e = {"value": problems_total / (e2e_ms / 1e3), "unit": "problems/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": int(R * 5 * 8)}
 
     line = {"metric": METRIC, "value": value, "unit": "problems/s (NS run + adjoint)", "n_gpus": world,
@@ -672,7 +670,7 @@ def main_blr(args):
             "data": "synthetic (seeded)",
             "config": {"workload": wdesc, "problems_per_gpu": R, "warmup_steps": "init + 2 iterations + adjoint",
                        "l2": "per-step sample stores > L2 (no flush needed)"},
-            "likelihood_evals_per_s": nevals * world / (ms / 1e3), "gpu_launches": int(gpu_launches),
+            "likelihood_evals_per_s": nevals / (ms / 1e3), "gpu_launches": int(gpu_launches),
             "roofline": roofline, "e2e": e2e, "clocks": clk.summary(), "accuracy": accuracy,
             "iterations": {"max": int(st["iterations"].max()), "mean": float(st["iterations"].mean())},
             "information_H": {"min": float(min(p["H"] for p in wl)), "max": float(max(p["H"] for p in wl))}}
