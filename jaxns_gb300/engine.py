@@ -1,5 +1,5 @@
 """Batched nested-sampling engine: device buffers of many independent runs and the
-iteration driver over libgbns.so.
+iteration loop over libgbns.so.
 
 One ``NSBatch`` holds R runs (uneven D, n, store size) in packed structure-of-arrays
 buffers.  ``run()`` initialises the live points, then replays a captured CUDA graph of
