@@ -219,6 +219,9 @@ def main():
                     help="config3: keep only runs of this dimension (repeated to --runs); for kernel profiling")
     ap.add_argument("--plain-problems", type=int, default=3,
                     help="blr workloads: problems in the plain GPU + finite-difference comparison")
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the sampler's launch shapes on the batch first (default for config3)")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-e2e", action="store_true",
                     help="blr workloads: skip the end-to-end pass (one more full step)")
     ap.add_argument("--kernel-profile", action="store_true",
@@ -282,7 +285,9 @@ def main():
     from jaxns_gb300.replicas import reduce_timing, replica_keys
     samplers = make_samplers(wl)
     keys = replica_keys(rank, len(wl))  # independent seeds on every rank
-    bns = BatchedNestedSampler(samplers, keys, [gb.TerminationCondition(dlogZ=1e-4)] * len(wl), block=args.block)
+    tune = args.autotune or (args.workload == "config3" and not args.no_autotune)
+    bns = BatchedNestedSampler(samplers, keys, [gb.TerminationCondition(dlogZ=1e-4)] * len(wl), block=args.block,
+                               autotune=tune)
     b = bns.batch
     if args.iterations is not None:
         # kernel-profiling mode: init + a fixed number of eager iterations, no results pass
@@ -386,7 +391,10 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (FP64 evidence)", "data": "synthetic (seeded)",
             "config": {"workload": wdesc, "runs_per_gpu": args.runs, "graph_block": args.block,
-                       "l2": "per-step sample store > L2 (no flush needed)"},
+                       "l2": "per-step sample store > L2 (no flush needed)",
+                       "launch_shape": ({k: bns.tuning[k] for k in ("chains_per_item", "wide_chains_per_item")}
+                                        if bns.tuning else {"chains_per_item": 64, "wide_chains_per_item": "default"}),
+                       "autotune_table": bns.tuning["table"] if bns.tuning else None},
             "likelihood_evals_per_s": evals_per_s, "gpu_launches": int(gpu_launches), "roofline": roofline,
             "e2e": e2e, "clocks": clocks, "accuracy": accuracy,
             "iterations": {"max": int(st["iterations"].max()), "mean": float(st["iterations"].mean())}}

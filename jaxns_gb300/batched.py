@@ -12,13 +12,14 @@ from typing import List, Optional, Sequence
 import numpy as np
 import torch
 
-from .engine import NSBatch
+from .engine import FAMILY_LINGAUSS, NSBatch
 from .public import NestedSampler, NestedSamplerResults, TerminationCondition, results_from_batch
 
 
 class BatchedNestedSampler:
     def __init__(self, samplers: Sequence[NestedSampler], keys, term_conds: Optional[Sequence] = None,
-                 block: int = 16, chains_per_item: int = 64, store_U: bool = False, lg_tensor_cores: bool = True):
+                 block: int = 16, chains_per_item: int = 64, store_U: bool = False, lg_tensor_cores: bool = True,
+                 autotune: bool = False, wide_chains_per_item: int = 0):
         self.samplers = list(samplers)
         keys = np.asarray(keys, np.uint32).reshape(len(self.samplers), 2)
         if term_conds is None:
@@ -29,7 +30,15 @@ class BatchedNestedSampler:
             spec.store_U = store_U
             specs.append(spec)
         self.block = int(block)
-        self.batch = NSBatch(specs, chains_per_item=chains_per_item, lg_tensor_cores=lg_tensor_cores)
+        self.tuning = None
+        if autotune and not any(s.family == FAMILY_LINGAUSS for s in specs):
+            # launch shapes timed on this batch (results do not depend on them)
+            from .autotune import autotune_launch
+            self.tuning = autotune_launch(specs)
+            chains_per_item = self.tuning["chains_per_item"]
+            wide_chains_per_item = self.tuning["wide_chains_per_item"]
+        self.batch = NSBatch(specs, chains_per_item=chains_per_item, wide_chains_per_item=wide_chains_per_item,
+                             lg_tensor_cores=lg_tensor_cores)
         self.state = None
 
     def __call__(self, from_host: bool = True, use_graph: bool = True, check: bool = True,
