@@ -173,7 +173,7 @@ typedef struct {
     int max_evals_per_slice;        /* shrink-loop evaluation budget per slice */
     int gradient_guided;            /* UniDimSliceSampler(gradient_guided=True): after each accepted point
                                        the direction is reflected about the U-space gradient of log L
-                                       (thread-per-chain sampler: MVN D <= 16 and shells) */
+                                       (MVN and shells families) */
     int pad_gg;
 } gbns_batch;
 

@@ -462,6 +462,19 @@ __device__ __forceinline__ float prior_quantile(int kind, float a, float b, floa
   return fmaf(b, GBNS_SQRT2F * erfinvf(fmaf(2.0f, u, -1.0f)), a);
 }
 
+// Prior quantile x(u) and its slope dx/du (Uniform: b; Normal: b sqrt(2 pi) exp(z^2 / 2)),
+// for U-space gradients of log L.
+__device__ __forceinline__ void prior_quantile_slope(int kind, float a, float b, float u, float &x, float &dxdu) {
+  if (kind == GBNS_PRIOR_UNIFORM) {
+    x = fmaf(b, u, a);
+    dxdu = b;
+  } else {
+    const float z = GBNS_SQRT2F * erfinvf(fmaf(2.0f, u, -1.0f));
+    x = fmaf(b, z, a);
+    dxdu = b * 2.5066282746310002f * __expf(0.5f * z * z);
+  }
+}
+
 // The same of an FP64 u (the linear-Gaussian family's U space).
 __device__ __forceinline__ float prior_quantile_d(int kind, float a, float b, double u) {
   if (kind == GBNS_PRIOR_UNIFORM) return (float)((double)a + (double)b * u);

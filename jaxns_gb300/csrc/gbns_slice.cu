@@ -30,18 +30,8 @@ template <int DMAX, int FAM>
 __device__ __forceinline__ void grad_u(const RunSmem<DMAX, FAM> &P, int D, const float *u, float *g) {
   float x[DMAX], dxdu[DMAX];
 #pragma unroll
-  for (int j = 0; j < DMAX; ++j) {
-    if (j < D) {
-      if (P.kind[j] == GBNS_PRIOR_UNIFORM) {
-        x[j] = fmaf(P.b[j], u[j], P.a[j]);
-        dxdu[j] = P.b[j];
-      } else {
-        const float z = GBNS_SQRT2F * erfinvf(fmaf(2.0f, u[j], -1.0f));
-        x[j] = fmaf(P.b[j], z, P.a[j]);
-        dxdu[j] = P.b[j] * 2.5066282746310002f * __expf(0.5f * z * z);
-      }
-    }
-  }
+  for (int j = 0; j < DMAX; ++j)
+    if (j < D) prior_quantile_slope(P.kind[j], P.a[j], P.b[j], u[j], x[j], dxdu[j]);
   if (FAM == GBNS_LIK_MVN) {
     float e[DMAX], z[DMAX];
 #pragma unroll

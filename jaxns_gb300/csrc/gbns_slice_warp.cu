@@ -38,7 +38,11 @@ __device__ __forceinline__ float slice_alpha_w(int j, int S) {
   return 0.5f * (1.0f - step) + step;
 }
 
-template <int DMAX>
+// GRAD: the gradient-guided variant.  After each accepted point the chain's direction is
+// reflected about the U-space gradient of log L there (uni_slice_sampler.py:255-269), computed
+// warp-cooperatively: e = x - mu, z = Linv e, g = -Linv^T z (lanes over dimensions, the
+// vectors staged in two columns of the proposal scratch), times the prior quantile's slope.
+template <int DMAX, bool GRAD>
 __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PER_CTA_32))
     k_slice_mvn_warp(gbns_batch b, int item_begin, const float *__restrict__ Lstar_in,
                      const uint32_t *__restrict__ keys_in) {
@@ -303,6 +307,58 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
       }
     }
     __syncwarp();
+    bool grad_fallback = false;
+    if (GRAD) {
+      // reflect each advancing chain's direction about the gradient at its accepted point
+      unsigned mm = am;
+      while (mm) {
+        const int q = __ffs(mm) - 1;
+        mm &= mm - 1;
+        float e0 = 0.f, e1 = 0.f, s0 = 0.f, s1 = 0.f;
+        if (j0 < D) {
+          float x;
+          prior_quantile_slope(pkind[j0], pa[j0], pb[j0], V.U0[j0][q], x, s0);
+          e0 = x - pmu[j0];
+        }
+        if (DMAX > 32 && j1 < D) {
+          float x;
+          prior_quantile_slope(pkind[j1], pa[j1], pb[j1], V.U0[j1][q], x, s1);
+          e1 = x - pmu[j1];
+        }
+        V.DEL[j0][0] = e0;
+        if (DMAX > 32) V.DEL[j1][0] = e1;
+        __syncwarp();
+        float z0 = 0.f, z1 = 0.f;  // z = Linv e, rows j0, j1
+        for (int k = 0; k < D; ++k) {
+          const float ek = V.DEL[k][0];
+          z0 = fmaf(LinvT[k * DMAX + j0], ek, z0);
+          if (DMAX > 32) z1 = fmaf(LinvT[k * DMAX + j1], ek, z1);
+        }
+        V.DEL[j0][1] = z0;
+        if (DMAX > 32) V.DEL[j1][1] = z1;
+        __syncwarp();
+        float g0 = 0.f, g1 = 0.f;  // -Linv^T z, rows j0, j1
+        for (int i = 0; i < D; ++i) {
+          const float zi = V.DEL[i][1];
+          g0 = fmaf(LinvT[j0 * DMAX + i], zi, g0);
+          if (DMAX > 32) g1 = fmaf(LinvT[j1 * DMAX + i], zi, g1);
+        }
+        g0 = -g0 * s0;
+        g1 = -g1 * s1;
+        const float gn = sqrtf(warp_sum(fmaf(g0, g0, g1 * g1)));
+        if (!(gn >= 1e-10f) || isinf(gn)) {
+          if (lane == q) grad_fallback = true;
+        } else {
+          const float d0 = j0 < D ? V.DIR[j0][q] : 0.f, d1 = (DMAX > 32 && j1 < D) ? V.DIR[j1][q] : 0.f;
+          const float dot = warp_sum(fmaf(d0, g0 / gn, d1 * (g1 / gn)));
+          const float r0 = fmaf(-2.0f * dot, g0 / gn, d0), r1 = fmaf(-2.0f * dot, g1 / gn, d1);
+          const float rn = sqrtf(warp_sum(fmaf(r0, r0, r1 * r1)));
+          if (j0 < D) V.DIR[j0][q] = r0 / rn;
+          if (DMAX > 32 && j1 < D) V.DIR[j1][q] = r1 / rn;
+        }
+        __syncwarp();
+      }
+    }
     if (advance) {
       logL0 = logL;
       const int p = j - (S - 1 - K);
@@ -313,9 +369,15 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
       }
       ++j;
       start = true;
+      if (GRAD) ++total;  // the gradient counts as one likelihood evaluation
       if (j < S) {
-        need_dir = true;
-        dir_key = after_key;
+        if (!GRAD) {
+          need_dir = true;
+          dir_key = after_key;
+        } else if (grad_fallback) {
+          need_dir = true;
+          dir_key = fold(after_key, 0u);  // split(after_key)[0]
+        }
       } else {
         // chain finished: outputs, then the next chain of the pool
         const size_t out = (size_t)rd.shell_off + c;
@@ -347,20 +409,21 @@ static cudaError_t launch_warp_bucket(const gbns_batch &b, int ib, int ie, const
   const size_t sm = warp_smem_bytes<DMAX>(warps);
   static bool configured = false;
   if (!configured) {
-    cudaError_t e = cudaFuncSetAttribute(k_slice_mvn_warp<DMAX>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    cudaError_t e = cudaFuncSetAttribute(k_slice_mvn_warp<DMAX, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sm);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(k_slice_mvn_warp<DMAX, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  k_slice_mvn_warp<DMAX><<<nblk, 32 * warps, sm, stream>>>(b, ib, Lstar, keys);
+  if (b.gradient_guided) k_slice_mvn_warp<DMAX, true><<<nblk, 32 * warps, sm, stream>>>(b, ib, Lstar, keys);
+  else k_slice_mvn_warp<DMAX, false><<<nblk, 32 * warps, sm, stream>>>(b, ib, Lstar, keys);
   return cudaGetLastError();
 }
 
 // MVN buckets 2 (16 < D <= 32) and 3 (32 < D <= 64) run here.
 cudaError_t launch_slice_warp(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream) {
   cudaError_t e;
-  // the gradient-guided slice runs on the thread-per-chain kernel only (MVN D <= 16)
-  if (b.gradient_guided && (b.bucket_end[2] > b.bucket_begin[2] || b.bucket_end[3] > b.bucket_begin[3]))
-    return cudaErrorNotSupported;
   if ((e = launch_warp_bucket<32>(b, b.bucket_begin[2], b.bucket_end[2], Lstar, keys, stream))) return e;
   if ((e = launch_warp_bucket<64>(b, b.bucket_begin[3], b.bucket_end[3], Lstar, keys, stream))) return e;
   return cudaSuccess;

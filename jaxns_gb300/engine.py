@@ -144,10 +144,8 @@ class NSBatch:
         if len(gg) > 1:
             raise ValueError("a batch holds either gradient-guided runs only or none")
         self.gradient_guided = gg.pop()
-        if self.gradient_guided and any(s.family == FAMILY_LINGAUSS or (s.family == FAMILY_MVN and s.D > 16)
-                                        for s in specs):
-            raise NotImplementedError("the gradient-guided slice runs on the thread-per-chain sampler: "
-                                      "correlated Gaussians with D <= 16 and Gaussian shells")
+        if self.gradient_guided and any(s.family == FAMILY_LINGAUSS for s in specs):
+            raise NotImplementedError("the gradient-guided slice is not on the linear-Gaussian lock step")
         for s in specs:
             _dbucket(s.D)
         live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])

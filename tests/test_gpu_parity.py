@@ -198,7 +198,8 @@ def test_evidence_stats_fp64(gpu_lib, oracle_mod):
         np.testing.assert_allclose(lZ.cpu().numpy(), oper["log_Z_mean"], rtol=1e-6, atol=1e-5)
 
 
-@pytest.mark.parametrize("D,n,S,bar", [(4, 128, 2, 0.97), (12, 256, 3, 0.97), (4, 128, 16, 0.75), (12, 256, 24, 0.75)])
+@pytest.mark.parametrize("D,n,S,bar", [(4, 128, 2, 0.97), (12, 256, 3, 0.97), (24, 128, 3, 0.97), (40, 96, 3, 0.97),
+                                       (4, 128, 16, 0.75), (12, 256, 24, 0.75)])
 def test_gradient_guided_chain_parity(gpu_lib, oracle_mod, D, n, S, bar):
     """UniDimSliceSampler(gradient_guided=True) (uni_slice_sampler.py:255-269): after every
     accepted point the direction is reflected about the U-space gradient (one extra evaluation
