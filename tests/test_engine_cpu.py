@@ -1,0 +1,88 @@
+"""Host-side batch layout of NSBatch, built on the CPU (no kernel runs): work items cover every
+chain exactly once, the items of each (family, D) bucket are contiguous, packed offsets are
+exclusive prefix sums of the per-run sizes, and the linear-Gaussian family stores U as FP64
+word pairs."""
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+
+def _specs():
+    from jaxns_gb300.engine import FAMILY_LINGAUSS, FAMILY_MVN, FAMILY_SHELLS, RunSpec
+    out = []
+    rng = np.random.default_rng(0)
+    for i, (fam, D, n) in enumerate([(FAMILY_MVN, 4, 64), (FAMILY_MVN, 12, 200), (FAMILY_MVN, 20, 96),
+                                     (FAMILY_MVN, 40, 128), (FAMILY_SHELLS, 6, 80), (FAMILY_SHELLS, 50, 100)]):
+        s = n // 2
+        out.append(RunSpec(D=D, num_live_points=n, shell_size=s, num_slices=2 * D, family=fam,
+                           params=rng.standard_normal(D * D + 3 * D + 3).astype(np.float32),
+                           prior_kind=np.zeros(D, np.int32), prior_a=np.zeros(D), prior_b=np.ones(D),
+                           max_samples=10 * n, term_cond={"dlogZ": 1e-4, "max_samples": 10.0 * n},
+                           key=np.array([0, i], np.uint32), store_U=(i % 2 == 0)))
+    return out
+
+
+def test_items_cover_every_chain_once_and_buckets_are_contiguous():
+    from jaxns_gb300.engine import NSBatch, _dbucket
+    specs = _specs()
+    for cpi, wide in ((32, 0), (64, 256), (128, 512)):
+        b = NSBatch(specs, device="cpu", chains_per_item=cpi, wide_chains_per_item=wide)
+        items = b.items.numpy()[: b._b.num_items]
+        covered = [np.zeros(s.shell_size, np.int32) for s in specs]
+        for r, c0, cnt, _ in items:
+            covered[r][c0:c0 + cnt] += 1
+            wide_run = specs[r].family == 0 and specs[r].D > 16
+            assert cnt <= (wide or (256 if specs[r].D > 32 else 512)) if wide_run else cnt <= cpi
+        assert all(np.all(c == 1) for c in covered)
+        for k in range(8):
+            lo, hi = b._b.bucket_begin[k], b._b.bucket_end[k]
+            for r, *_ in items[lo:hi]:
+                assert specs[r].family * 4 + _dbucket(specs[r].D) == k
+        assert sum(b._b.bucket_end[k] - b._b.bucket_begin[k] for k in range(8)) == len(items)
+
+
+def test_packed_offsets_are_exclusive_prefix_sums():
+    from jaxns_gb300.engine import NSBatch
+    specs = _specs()
+    b = NSBatch(specs, device="cpu")
+    ns = np.array([s.num_live_points for s in specs])
+    ss = np.array([s.shell_size for s in specs])
+    caps = np.array([s.max_samples for s in specs])
+    Ds = np.array([s.D for s in specs])
+    excl = lambda v: np.concatenate([[0], np.cumsum(v)[:-1]])
+    np.testing.assert_array_equal(b.offsets["live"], excl(ns))
+    np.testing.assert_array_equal(b.offsets["shell"], excl(ss))
+    np.testing.assert_array_equal(b.offsets["store"], excl(caps))
+    np.testing.assert_array_equal(b.offsets["liveU"], excl(ns * Ds))
+    ustore = np.array([s.store_U for s in specs])
+    ucap = np.where(ustore, caps * Ds, 0)
+    np.testing.assert_array_equal(b.offsets["ustore"], np.where(ustore, excl(ucap), -1))
+    assert b.live_U[0].numel() == int((ns * Ds).sum()) and b.store_L.numel() == int(caps.sum())
+
+
+def test_lingauss_runs_keep_fp64_U_as_word_pairs():
+    from jaxns_gb300.engine import FAMILY_LINGAUSS, NSBatch, RunSpec
+    N, P, n = 50, 3, 20
+    rng = np.random.default_rng(1)
+    spec = RunSpec(D=P, num_live_points=n, shell_size=n // 2, num_slices=2 * P, family=FAMILY_LINGAUSS,
+                   params=np.concatenate([rng.standard_normal(N * P), rng.standard_normal(N), [0.5]]).astype(np.float32),
+                   prior_kind=np.ones(P, np.int32), prior_a=np.zeros(P), prior_b=np.ones(P), max_samples=200,
+                   term_cond={"dlogZ": 1e-4, "max_samples": 200.0}, key=np.array([0, 1], np.uint32), N=N)
+    b = NSBatch([spec], device="cpu", lg_tensor_cores=False)
+    assert int(b.ucols[0]) == 2 * P
+    assert b.live_U[0].numel() == n * 2 * P and b.new_U.numel() == (n // 2) * 2 * P
+    assert b.live_view(0)["U"].dtype == torch.float64 and b.live_view(0)["U"].shape == (n, P)
+    assert b.lg_t["u0"].numel() == (n // 2) * P and b.lg_t["ss"].dtype == torch.float64
+
+
+def test_batch_mixing_rules():
+    from jaxns_gb300.engine import FAMILY_LINGAUSS, NSBatch
+    specs = _specs()
+    lg = _specs()[0]
+    lg.family, lg.N = FAMILY_LINGAUSS, 10
+    with pytest.raises(ValueError):
+        NSBatch([specs[0], lg], device="cpu", lg_tensor_cores=False)
+    specs[1].gradient_guided = True
+    with pytest.raises(ValueError):
+        NSBatch(specs, device="cpu")
