@@ -246,10 +246,10 @@ def main():
         wl = [pool[i % len(pool)] for i in range(args.runs)]
     threads = os.cpu_count() or 1
     if args.workload == "shells":
-        wdesc = (f"configs[1] Gaussian shells D=10 (R=2, w=0.1, centres +-3.5 e0, U[-6,6]^10), 1000 live points, "
+        wdesc = (f"Gaussian shells D=10 (R=2, w=0.1, centres +-3.5 e0, U[-6,6]^10), 1000 live points, "
                  f"50 slices, dlogZ<1e-4; {args.runs} independent seeds per GPU in one batched launch")
     else:
-        wdesc = (f"configs[2] batched correlated Gaussians: {args.runs} runs per GPU, D~U{{2..64}}, n=50D, S=5D, "
+        wdesc = (f"batched correlated Gaussians: {args.runs} runs per GPU, D~U{{2..64}}, n=50D, S=5D, "
                  f"dlogZ<1e-4")
 
     if args.impl == "reference":
@@ -516,9 +516,9 @@ def main_blr(args):
     if args.runs is None:
         args.runs = 1 if name == "blr" else 256
     threads = os.cpu_count() or 1
-    wdesc = ("configs[3] Bayesian linear regression: Phi 4096x32 ~ N(0,1), w ~ N(0,I), sigma=0.5, tau=1, 1024 live "
+    wdesc = ("Bayesian linear regression: Phi 4096x32 ~ N(0,1), w ~ N(0,I), sigma=0.5, tau=1, 1024 live "
              "points, num_slices=5P, default termination; NS run + reweighted-evidence adjoint" if name == "blr" else
-             f"configs[4] batched linear-regression evidence: {args.runs} problems per GPU, N~U[512,16384], "
+             f"batched linear-regression evidence: {args.runs} problems per GPU, N~U[512,16384], "
              f"P~U[8,64], sigma~U[0.1,1], tau~U[0.5,2], 25P live points, num_slices=5P; NS runs + adjoints")
     if args.impl == "reference":
         if rank == 0:
