@@ -125,12 +125,13 @@ __device__ __forceinline__ float slice_alpha(int j, int S) {
 }
 
 // Minimum resident CTAs per SM (8 caps registers at 64): the sampler is latency-bound, and
-// at DMAX <= 8 the cap costs at most 8 B of spills per thread; Gaussian shells at DMAX 16 runs
-// 4.8 % faster capped (172 B of spills) than at its natural 112 registers (4 CTAs per SM).
-// The other instantiations keep the occupancy they reach without a cap (3 or 4 CTAs).
+// at DMAX <= 8 the cap costs a few tens of bytes of spills per thread; Gaussian shells at
+// DMAX 16 runs fastest at 6 CTAs (80 registers, 52 B of spills): 2.8 % faster than at 8 CTAs
+// (64 registers, 194 B of spills) and 8 % faster than at its natural 112 registers.  The
+// other instantiations keep the occupancy they reach without a cap (3 or 4 CTAs).
 template <int DMAX, int FAM>
 constexpr int slice_min_blocks() {
-  return (DMAX <= 8 || (DMAX == 16 && FAM == GBNS_LIK_SHELLS)) ? 8 : (DMAX >= 64 ? 3 : 4);
+  return DMAX <= 8 ? 8 : ((DMAX == 16 && FAM == GBNS_LIK_SHELLS) ? 6 : (DMAX >= 64 ? 3 : 4));
 }
 
 // GRAD: the gradient-guided variant (the direction of slice j + 1 is the reflection of slice
@@ -192,6 +193,8 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
   const int c = c_begin + (valid ? threadIdx.x : 0);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __shared__ float dirbuf[4][32][DMAX + 1];
+  __shared__ uint4 dirkey[4][32];  // (direction key, lane) of each lane that needs a direction
+  const uint32_t dmagic = ((1u << 20) + (uint32_t)D - 1u) / (uint32_t)D;  // p / D = p * dmagic >> 20 for p < 2^14
 
   // --- keys: _collect_shell split (sharded_static.py:248) then split(sample_key, s)[c]
   Key sample_key;
@@ -241,22 +244,21 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
   bool failed = false;
   for (;;) {
     // ---- new directions: the D normals of every lane that needs one, flattened over
-    // (lane, dimension) pairs across the warp
+    // (lane, dimension) pairs across the warp; lanes publish their keys in rank order
     const unsigned dmask = __ballot_sync(0xffffffffu, need_dir);
     if (dmask) {
       if (D == 1) {
         if (need_dir) d[0] = 1.0f;
       } else {
+        if (need_dir)
+          dirkey[wid][__popc(dmask & ((1u << lane) - 1u))] = make_uint4(dir_key.k0, dir_key.k1, (uint32_t)lane, 0u);
+        __syncwarp();
         const int cnt = __popc(dmask) * D;
-        for (int base = 0; base < cnt; base += 32) {
-          const int p = base + lane;
-          const bool ok = p < cnt;
-          const int src = ok ? (int)__fns(dmask, 0u, p / D + 1) : 0;
-          const Key dk = {__shfl_sync(0xffffffffu, dir_key.k0, src), __shfl_sync(0xffffffffu, dir_key.k1, src)};
-          if (ok) {
-            const int jj = p % D;
-            dirbuf[wid][src][jj] = normal_from_bits(bits64(dk, (uint32_t)jj));
-          }
+        for (int p = lane; p < cnt; p += 32) {
+          const int g = (int)(((uint32_t)p * dmagic) >> 20);
+          const uint4 e = dirkey[wid][g];
+          const uint32_t jj = (uint32_t)(p - g * D);
+          dirbuf[wid][e.z][jj] = normal_from_bits(bits64(Key{e.x, e.y}, jj));
         }
         __syncwarp();
         if (need_dir) {
