@@ -1,8 +1,9 @@
 /*
  * gbns.h -- C ABI of libgbns.so, the GB300 (sm_103a) nested-sampling inner loop.
  *
- * All pointers named *_dev are device pointers; the caller owns every buffer (sizes from
- * gbns_batch_layout).  The library never allocates device memory inside a run, never
+ * All pointers named *_dev are device pointers; the caller owns every buffer (the packed
+ * per-run offsets and sizes are the caller's layout, e.g. jaxns_gb300/engine.py NSBatch;
+ * gbns_abi_sizes reports the struct sizes).  The library never allocates device memory inside a run, never
  * synchronises inside gbns_batch_iterate, and reports errors through the return code
  * (0 = OK, negative = argument/launch error; message from gbns_last_error()).
  * Per-run device status words (gbns_run_state.status) carry budget/overflow errors.
