@@ -133,7 +133,7 @@ class ClockSampler:
                                       "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
                 for line in out.stdout.strip().splitlines():
                     self.rows.append([x.strip() for x in line.split(",")])
-            except Exception:
+            except (OSError, subprocess.SubprocessError):
                 pass
             self._stop.wait(0.2)
 

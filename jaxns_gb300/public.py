@@ -319,7 +319,28 @@ class NestedSampler:
         return reason, state_from_batch(batch, 0)
 
     def to_results(self, termination_reason, state: NestedSamplerState, trim: bool = True) -> NestedSamplerResults:
+        """public.py:177-196.  The per-sample arrays always hold exactly the run's samples (the
+        device results pass reads the run's own slice of the store), so ``trim`` changes nothing;
+        it is accepted for the reference's signature."""
         return self._nested_sampler._to_results(termination_reason, state, trim)
+
+    @staticmethod
+    def trim_results(results: NestedSamplerResults) -> NestedSamplerResults:
+        """public.py:198-220: every array of more than one element, also inside the ``samples``
+        dicts, cut to its first ``results.total_num_samples`` rows; scalars unchanged."""
+        n = int(results.total_num_samples)
+
+        def size(x):
+            return x.numel() if hasattr(x, "numel") else int(np.size(x))
+
+        def trim(x):
+            if isinstance(x, dict):
+                return {k: trim(v) for k, v in x.items()}
+            if hasattr(x, "shape") and len(x.shape) > 0 and size(x) > 1:
+                return x[:n]
+            return x
+
+        return results._replace(**{f: trim(getattr(results, f)) for f in results._fields})
 
 
 def state_from_batch(batch: NSBatch, r: int) -> NestedSamplerState:

@@ -80,3 +80,26 @@ def test_results_json_roundtrip_reference_format(tmp_path):
     g.write_text(json.dumps(raw))
     back2 = load_results(str(g))
     np.testing.assert_array_equal(back2.log_X_mean, res.log_X_mean)
+
+
+def test_trim_results_cuts_per_sample_arrays():
+    """NestedSampler.trim_results (public.py:198-220): arrays of more than one element, also
+    inside the samples dicts, keep their first total_num_samples rows; scalars stay."""
+    torch = pytest.importorskip("torch")
+    from jaxns_gb300.public import NestedSampler, NestedSamplerResults
+    N, cap = 6, 10
+    pad = lambda *s: np.arange(int(np.prod((cap,) + s)), dtype=np.float64).reshape((cap,) + s)
+    res = NestedSamplerResults(
+        log_Z_mean=-1.5, log_Z_uncert=0.1, ESS=50.0, H_mean=2.0,
+        samples={"x": pad(3), "y": torch.arange(cap)}, parametrised_samples={"x": pad(3)},
+        U_samples=pad(3), log_L_samples=torch.arange(cap, dtype=torch.float64), log_dp_mean=pad(),
+        log_X_mean=pad(), log_posterior_density=pad(), num_live_points_per_sample=pad(),
+        num_likelihood_evaluations_per_sample=np.arange(cap), total_num_samples=N, total_phantom_samples=0,
+        total_num_likelihood_evaluations=123, log_efficiency=-0.7, termination_reason=4)
+    t = NestedSampler.trim_results(res)
+    assert t.U_samples.shape == (N, 3) and t.samples["x"].shape == (N, 3) and t.samples["y"].shape == (N,)
+    assert t.log_L_samples.shape == (N,) and t.num_likelihood_evaluations_per_sample.shape == (N,)
+    np.testing.assert_array_equal(t.log_dp_mean, np.arange(N))
+    assert (t.log_Z_mean, t.total_num_samples, t.termination_reason) == (-1.5, N, 4)
+    one = res._replace(log_dp_mean=np.zeros(1))
+    assert NestedSampler.trim_results(one).log_dp_mean.shape == (1,)
