@@ -112,6 +112,19 @@ def load(path: str = LIB_PATH):
     return lib
 
 
+def require_cuda(what: str, **tensors):
+    """Raise unless every named tensor lives on one CUDA device: the kernels take device
+    pointers, and a host pointer must never reach them (there is no CPU path)."""
+    devs = set()
+    for name, t in tensors.items():
+        if not getattr(t, "is_cuda", False):
+            raise GBNSError(f"{what}: {name} is on {getattr(t, 'device', type(t).__name__)}; the kernels need CUDA "
+                            "device buffers (there is no CPU path)")
+        devs.add(t.device)
+    if len(devs) > 1:
+        raise GBNSError(f"{what}: tensors on several devices {sorted(map(str, devs))}")
+
+
 def call(name: str, *args):
     lib = load()
     rc = getattr(lib, name)(*args)

@@ -42,6 +42,7 @@ def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float, tensor_core
     tensor_cores: the per-point residuals |y - Phi w|^2 as a 3xTF32 tcgen05 GEMM
     (gbns_evidence_adjoint_tc) instead of fp32 CUDA-core tiles (gbns_evidence_adjoint).
     check: synchronise and raise if a tensor-core wait timed out."""
+    _ffi.require_cuda("evidence_and_grad", U=ds.U, log_w=ds.log_w, Phi=ds.Phi, y=ds.y)
     M, P = ds.U.shape
     N = ds.Phi.shape[0]
     dev = ds.U.device
@@ -49,7 +50,7 @@ def evidence_and_grad(ds: DeadSet, log_tau: float, log_sigma: float, tensor_core
     ss = torch.empty(max(M, 1), dtype=torch.float64, device=dev)
     ry = torch.empty(max(M, 1), dtype=torch.float64, device=dev)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
-    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     args = [p(ds.U), p(ds.log_w), ctypes.c_longlong(M), ctypes.c_int(P), p(ds.Phi), p(ds.y), ctypes.c_int(N),
             ctypes.c_double(float(log_tau)), ctypes.c_double(float(log_sigma)), p(out), p(ss), p(ry)]
     if not tensor_cores:
@@ -70,6 +71,8 @@ def batch_evidence_and_grad(batch, results, thetas, tensor_cores: bool = True, c
     device results pass (NSBatch.results(with_U=True)); thetas: [R, 2] (log tau, log sigma).
     Phi and y are read in place from the batch's parameter buffer.  Returns [R, 3] FP64 on
     the device: log Z(theta), d/d log tau, d/d log sigma."""
+    if batch.device.type != "cuda":
+        raise _ffi.GBNSError(f"batch_evidence_and_grad: the batch is on {batch.device} (there is no CPU path)")
     st = batch.state()
     R = batch.R
     dev = batch.device
@@ -84,7 +87,7 @@ def batch_evidence_and_grad(batch, results, thetas, tensor_cores: bool = True, c
     ws = torch.empty(max(2 * Mmax * 64, 1), dtype=torch.float32, device=dev)
     ps = torch.empty(2 * Nmax * 64, dtype=torch.float32, device=dev)
     status = torch.zeros(1, dtype=torch.int32, device=dev)
-    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    stream = ctypes.c_void_p(torch.cuda.current_stream(dev).cuda_stream)
     p = lambda t: ctypes.c_void_p(t.data_ptr())
     log_Z = results["scalars"][:, 0]
     log_w_all = results["log_dp_mean"] - results["log_L_samples"]

@@ -338,9 +338,13 @@ class NSBatch:
         return g
 
     # ----------------------------------------------------------------- driving
-    @staticmethod
-    def _stream():
-        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    def _stream(self):
+        """The current CUDA stream of the batch's device; a batch built on the CPU (layout only)
+        refuses to launch anything."""
+        if self.device.type != "cuda":
+            raise _ffi.GBNSError(f"NSBatch on {self.device} holds host buffers; the kernels need a CUDA device "
+                                 "(there is no CPU path)")
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
     def init(self):
         _ffi.call("gbns_batch_init", ctypes.byref(self._b), self._stream())

@@ -86,3 +86,24 @@ def test_batch_mixing_rules():
     specs[1].gradient_guided = True
     with pytest.raises(ValueError):
         NSBatch(specs, device="cpu")
+
+
+def test_cpu_batch_refuses_to_launch():
+    """A batch built on the CPU (layout only) never hands host buffers to a kernel."""
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.engine import NSBatch
+    b = NSBatch(_specs(), device="cpu")
+    for call in (b.init, lambda: b.iterate(1), b.finalize, lambda: b.results(with_U=False)):
+        with pytest.raises(_ffi.GBNSError, match="no CPU path"):
+            call()
+
+
+def test_adjoint_refuses_host_tensors():
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.adjoint import DeadSet, evidence_and_grad
+    ds = DeadSet(U=torch.rand(10, 3, dtype=torch.float64), log_w=torch.zeros(10, dtype=torch.float64),
+                 Phi=torch.randn(20, 3), y=torch.randn(20))
+    with pytest.raises(_ffi.GBNSError, match="no CPU path"):
+        evidence_and_grad(ds, 0.0, 0.0)
+    with pytest.raises(_ffi.GBNSError, match="U is on"):
+        _ffi.require_cuda("x", U=np.zeros(3))
