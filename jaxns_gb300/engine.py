@@ -609,8 +609,12 @@ class NSBatch:
     def forward(self, r: int, U: torch.Tensor) -> torch.Tensor:
         """Model.forward of run r over a batch U [B, D] (device tensor; FP64 for the
         linear-Gaussian family)."""
+        if not 0 <= r < self.R:
+            raise ValueError(f"run {r} out of range [0, {self.R})")
         dt = torch.float64 if self.specs[r].family == FAMILY_LINGAUSS else torch.float32
         U = U.to(device=self.device, dtype=dt).contiguous()
+        if U.dim() != 2 or U.shape[1] != self.specs[r].D:
+            raise ValueError(f"U must be [B, {self.specs[r].D}] for run {r}, got {tuple(U.shape)}")
         out = torch.empty(U.shape[0], dtype=torch.float32, device=self.device)
         _ffi.call("gbns_forward", ctypes.byref(self._b), int(r), ctypes.c_void_p(U.data_ptr()),
                   ctypes.c_void_p(out.data_ptr()), ctypes.c_longlong(U.shape[0]), self._stream())
@@ -622,6 +626,9 @@ class NSBatch:
         hook): outputs in new_U / new_L (relative) / new_E."""
         Lstar = Lstar.to(device=self.device, dtype=torch.float32).contiguous()
         keys = keys.to(device=self.device, dtype=torch.int32).contiguous()
+        if Lstar.numel() != self.R or keys.numel() != 2 * self.R:
+            raise ValueError(f"need one contour and one key (2 words) per run: {self.R} runs, got "
+                             f"{Lstar.numel()} contours and {keys.numel()} key words")
         _ffi.call("gbns_slice_shell", ctypes.byref(self._b), ctypes.c_void_p(Lstar.data_ptr()),
                   ctypes.c_void_p(keys.data_ptr()), self._stream())
 

@@ -107,3 +107,17 @@ def test_adjoint_refuses_host_tensors():
         evidence_and_grad(ds, 0.0, 0.0)
     with pytest.raises(_ffi.GBNSError, match="U is on"):
         _ffi.require_cuda("x", U=np.zeros(3))
+
+
+def test_hook_shapes_are_checked_on_the_host():
+    from jaxns_gb300.engine import NSBatch
+    specs = _specs()
+    b = NSBatch(specs, device="cpu")
+    with pytest.raises(ValueError, match="out of range"):
+        b.forward(len(specs), torch.zeros(3, specs[0].D))
+    with pytest.raises(ValueError, match=r"U must be \[B, 4\]"):
+        b.forward(0, torch.zeros(3, 5))
+    with pytest.raises(ValueError, match="one contour and one key"):
+        b.slice_shell(torch.zeros(len(specs) - 1), torch.zeros(len(specs), 2, dtype=torch.int32))
+    with pytest.raises(ValueError, match="one contour and one key"):
+        b.slice_shell(torch.zeros(len(specs)), torch.zeros(len(specs), dtype=torch.int32))
