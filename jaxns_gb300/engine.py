@@ -641,6 +641,8 @@ class NSBatch:
         o = int(self.offsets["live"][r])
         uo = int(self.offsets["liveU"][r])
         n = s.num_live_points
+        if np.shape(U) != (n, s.D) or np.shape(log_L) != (n,):
+            raise ValueError(f"run {r} needs U [{n}, {s.D}] and log_L [{n}], got {np.shape(U)} and {np.shape(log_L)}")
         dt = np.float64 if s.family == FAMILY_LINGAUSS else np.float32
         words = torch.from_numpy(np.ascontiguousarray(np.asarray(U, dt).ravel()).view(np.float32))
         self.live_U[p][uo:uo + n * int(self.ucols[r])].copy_(words)

@@ -74,6 +74,10 @@ def test_lingauss_runs_keep_fp64_U_as_word_pairs():
     assert b.live_U[0].numel() == n * 2 * P and b.new_U.numel() == (n // 2) * 2 * P
     assert b.live_view(0)["U"].dtype == torch.float64 and b.live_view(0)["U"].shape == (n, P)
     assert b.lg_t["u0"].numel() == (n // 2) * P and b.lg_t["ss"].dtype == torch.float64
+    U = np.random.default_rng(2).random((n, P))
+    U[0, 0] = 1e-300                                  # a value fp32 cannot hold
+    b.set_live(0, U, np.sort(rng.standard_normal(n)))
+    np.testing.assert_array_equal(b.live_view(0)["U"].numpy(), U)
 
 
 def test_batch_mixing_rules():
@@ -121,3 +125,22 @@ def test_hook_shapes_are_checked_on_the_host():
         b.slice_shell(torch.zeros(len(specs) - 1), torch.zeros(len(specs), 2, dtype=torch.int32))
     with pytest.raises(ValueError, match="one contour and one key"):
         b.slice_shell(torch.zeros(len(specs)), torch.zeros(len(specs), dtype=torch.int32))
+
+
+def test_set_live_writes_the_run_slice():
+    from jaxns_gb300.engine import NSBatch
+    specs = _specs()
+    b = NSBatch(specs, device="cpu")
+    r = 2
+    s = specs[r]
+    U = np.random.default_rng(0).random((s.num_live_points, s.D)).astype(np.float32)
+    L = np.sort(np.random.default_rng(1).standard_normal(s.num_live_points)).astype(np.float32)
+    with pytest.raises(ValueError):
+        b.set_live(r, U[:-1], L[:-1])
+    b.set_live(r, U, L)
+    v = b.live_view(r)
+    np.testing.assert_array_equal(v["U"].numpy(), U)
+    np.testing.assert_array_equal(v["log_L"].numpy(), L)
+    for q in range(len(specs)):      # the other runs' slices are untouched
+        if q != r:
+            assert not b.live_view(q)["log_L"].any()
