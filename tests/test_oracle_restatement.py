@@ -1,0 +1,174 @@
+"""A second, independent restatement of the slice sampler's chain (plain Python loops, written
+from the reference's source, small cases only) against the C oracle on the same keys.
+
+The C oracle is the checker for every GPU parity test, and jax cannot run here to pin it, so
+this test restates ``UniDimSliceSampler._get_sample`` once more, directly from
+samplers/bases.py:63-75, samplers/uni_slice_sampler.py:23-441 and internals/random.py:34-84,
+and requires bit-identical chains: seed index, every shrink step, the final point, its log L,
+the evaluation count and the phantoms.  Shared with the oracle are only the pinned primitives
+(threefry split and 64-bit words, checked against the Random123 known answers; the f64
+normal, checked against scipy's erfinv) and the model's log-likelihood, which is the model,
+not the sampler.
+
+Reduction orders, stated because jnp leaves them to XLA: the direction norm is a sequential sum
+of squares, and ``jnp.linspace(0.5, 1, S)[j]`` is ``0.5 (1 - j/(S-1)) + 1 (j/(S-1))`` with
+the last element exactly 1.
+"""
+import math
+import struct
+
+import numpy as np
+import pytest
+
+
+def _uniform(o, key):
+    """jax.random.uniform(key, (), float64): the top 52 of 64 random bits as the mantissa of a
+    float in [1, 2), minus 1."""
+    b = int(o.random_bits64(key, 1)[0])
+    f = struct.unpack("<d", struct.pack("<Q", (b >> 12) | 0x3FF0000000000000))[0] - 1.0
+    return max(0.0, f * (1.0 - 0.0) + 0.0)
+
+
+def _direction(o, key, D):
+    """_sample_direction (uni_slice_sampler.py:23-38)."""
+    if D == 1:
+        return np.ones(1)
+    d = np.asarray(o.normal(key, D), np.float64)
+    s = 0.0
+    for x in d:
+        s += x * x
+    return d / math.sqrt(s)
+
+
+def _bounds(U0, d):
+    """_slice_bounds (uni_slice_sampler.py:41-64)."""
+    t1 = (1.0 - U0) / d
+    t0 = -U0 / d
+    right = min(np.min(np.where(t0 >= 0, t0, np.inf)), np.min(np.where(t1 >= 0, t1, np.inf)))
+    left = max(np.max(np.where(t0 <= 0, t0, -np.inf)), np.max(np.where(t1 <= 0, t1, -np.inf)))
+    return float(left), float(right)
+
+
+def _alpha(j, S):
+    if S == 1:
+        return 0.5
+    if j == S - 1:
+        return 1.0
+    step = j / (S - 1)
+    return 0.5 * (1.0 - step) + 1.0 * step
+
+
+def _new_proposal(o, model, key, U0, logL0, d, midpoint, alpha, Lstar, trace):
+    """_new_proposal (uni_slice_sampler.py:114-273), perfect=True, no gradient options."""
+    run_key, _n_key, t_key, after_key = o.split(key, 4)
+    left, right = _bounds(U0, d)
+    t = left + _uniform(o, t_key) * (right - left)
+    U = U0 + t * d
+    logL = float(o.forward(model, U)[0])
+    ne = 1
+    k = run_key
+    trace.append((left, right, t))
+    while not ((logL > Lstar) or (logL0 == Lstar and logL == Lstar)):
+        k, t_key, _shrink_key = o.split(k, 3)
+        if t < 0:
+            left = t
+        if t > 0:
+            right = t
+        if midpoint:
+            if t < 0:
+                left = alpha * left
+            if t > 0:
+                right = alpha * right
+        t = left + _uniform(o, t_key) * (right - left)
+        U = U0 + t * d
+        logL = float(o.forward(model, U)[0])
+        ne += 1
+        trace.append((left, right, t))
+    return U, _direction(o, after_key, len(U0)), logL, ne
+
+
+def _seed_index(o, seed_key, live_logL, Lstar):
+    """get_seed_point -> sample_uniformly_masked -> resample_indicies(replace=True, S=1)
+    (internals/random.py:34-84); jax clamps an out-of-range gather index to the last row."""
+    log_w = np.where(live_logL > Lstar, 0.0, -np.inf)
+    cum = np.empty(len(log_w))
+    acc = -np.inf
+    for i, w in enumerate(log_w):
+        acc = np.logaddexp(acc, w)
+        cum[i] = acc
+    log_r = cum[-1] + math.log(1.0 - _uniform(o, seed_key))
+    return min(int(np.searchsorted(cum, log_r, side="left")), len(cum) - 1)
+
+
+def restated_get_sample(o, model, key, Lstar, live_U, live_logL, S, num_phantom, midpoint):
+    """BaseAbstractMarkovSampler._get_sample (bases.py:63-75) + get_sample_from_seed
+    (uni_slice_sampler.py:360-441)."""
+    sample_key, seed_key = o.split(key, 2)
+    idx = _seed_index(o, seed_key, live_logL, Lstar)
+    U, logL = live_U[idx].copy(), float(live_logL[idx])
+    direction_key, slices_key = o.split(sample_key, 2)
+    d = _direction(o, direction_key, live_U.shape[1])
+    keys = o.split(slices_key, S)
+    total, hist, trace = 0, [], []
+    for j in range(S):
+        U, d, logL, ne = _new_proposal(o, model, keys[j], U, logL, d, midpoint, _alpha(j, S), Lstar, trace)
+        total += ne
+        hist.append((U, logL))
+    phantoms = hist[-(num_phantom + 1):-1] if num_phantom else []
+    return idx, U, logL, total, phantoms, trace
+
+
+def _live_set(o, model, n, seed):
+    g = np.random.default_rng(seed)
+    U = g.random((n, model.D))
+    L = o.forward(model, U)
+    order = np.argsort(L, kind="stable")
+    return U[order], L[order]
+
+
+@pytest.mark.parametrize("family,D,S,k,midpoint", [("mvn", 2, 4, 0, True), ("mvn", 5, 10, 2, True),
+                                                   ("mvn", 8, 6, 0, False), ("shells", 3, 9, 3, True),
+                                                   ("shells", 1, 5, 1, True)])
+def test_restated_chain_is_bit_identical(oracle_mod, family, D, S, k, midpoint):
+    o = oracle_mod
+    g = np.random.default_rng(D * 100 + S)
+    if family == "mvn":
+        A = g.standard_normal((D, D))
+        model = o.mvn_model(np.full(D, -10.0), np.full(D, 10.0), g.standard_normal(D), A @ A.T / D + 0.1 * np.eye(D))
+    else:
+        c = np.zeros(D); c[0] = 3.5
+        model = o.shells_model(-6.0, 6.0, c, -c, 2.0, 0.5)
+    live_U, live_L = _live_set(o, model, 40, D)
+    for trial in range(12):
+        key = o.split(o.PRNGKey(1000 + trial), 2)[1]
+        s = int(g.integers(1, 30))
+        Lstar = float(live_L[s - 1])
+        idx, U, logL, ne, ph, trace = restated_get_sample(o, model, key, Lstar, live_U, live_L, S, k, midpoint)
+        U_o, L_o, ne_o, pU_o, pL_o = o.slice_get_sample(model, key, Lstar, live_U, live_L, S, num_phantom=k,
+                                                        midpoint_shrink=midpoint)
+        assert ne == ne_o and ne == len(trace), (trial, ne, ne_o)
+        np.testing.assert_array_equal(U, U_o)
+        assert logL == L_o and logL > Lstar
+        assert len(ph) == len(pL_o)
+        for (pu, pl), qu, ql in zip(ph, pU_o, pL_o):
+            np.testing.assert_array_equal(pu, qu)
+            assert pl == ql
+
+
+def test_restated_uniform_and_seed_index_match_the_oracle(oracle_mod):
+    o = oracle_mod
+    for seed in range(50):
+        key = o.PRNGKey(seed)
+        assert _uniform(o, key) == float(o.uniform(key, 1)[0])
+    g = np.random.default_rng(3)
+    import ctypes
+    f = o.lib().orc_seed_index_export
+    f.restype = ctypes.c_long
+    for trial in range(100):
+        n = int(g.integers(2, 300))
+        L = np.sort(g.standard_normal(n))
+        Lstar = float(L[int(g.integers(0, n - 1))])
+        key = o.split(o.PRNGKey(trial), 2)[1]
+        want = f(ctypes.c_uint32(int(key[0])), ctypes.c_uint32(int(key[1])),
+                 L.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_long(n), ctypes.c_double(Lstar))
+        assert _seed_index(o, key, L, Lstar) == want
