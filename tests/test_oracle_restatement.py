@@ -1,5 +1,6 @@
-"""A second, independent restatement of the slice sampler's chain (plain Python loops, written
-from the reference's source, small cases only) against the C oracle on the same keys.
+"""A second, independent restatement of the slice sampler's chain and of the FP64 evidence
+recurrence (plain Python, written from the reference's source, small cases only) against the C
+oracle on the same inputs.
 
 The C oracle is the checker for every GPU parity test, and jax cannot run here to pin it, so
 this test restates ``UniDimSliceSampler._get_sample`` once more, directly from
@@ -172,3 +173,87 @@ def test_restated_uniform_and_seed_index_match_the_oracle(oracle_mod):
         want = f(ctypes.c_uint32(int(key[0])), ctypes.c_uint32(int(key[1])),
                  L.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.c_long(n), ctypes.c_double(Lstar))
         assert _seed_index(o, key, L, Lstar) == want
+
+
+# ------------------------------------------------------------------ evidence statistics
+
+def _jnp_logaddexp(x1, x2):
+    """jnp.logaddexp for floats: max + log1p(exp(-|x1 - x2|)), x1 + x2 where the difference is
+    NaN (both infinite of one sign)."""
+    delta = x1 - x2
+    if math.isnan(delta):
+        return x1 + x2
+    return max(x1, x2) + math.log1p(math.exp(-abs(delta)))
+
+
+class _LS:
+    """The positive ("naked") LogSpace of internals/log_semiring.py: + is logaddexp (:147),
+    * adds logs (:181), ** n scales the log (:329)."""
+
+    def __init__(self, v):
+        self.v = float(v)
+
+    def __add__(self, o):
+        return _LS(_jnp_logaddexp(self.v, o.v))
+
+    def __mul__(self, o):
+        return _LS(self.v + o.v)
+
+    def __pow__(self, n):
+        return _LS(float(n) * self.v)
+
+
+def _restated_update(c, n, log_L_next):
+    """_update_evidence_calc_op (internals/shrinkage_statistics.py:43-94), its expressions as
+    written there, evaluated with Python's own operator associativity."""
+    LS = _LS
+    next_L = LS(log_L_next)
+    L_contour = LS(c["log_L"])
+    midL = LS(math.log(0.5)) * (next_L + L_contour)
+    X_mean, X2_mean, Z_mean = LS(c["log_X_mean"]), LS(c["log_X2_mean"]), LS(c["log_Z_mean"])
+    ZX_mean, Z2_mean, dZ2_mean = LS(c["log_ZX_mean"]), LS(c["log_Z2_mean"]), LS(c["log_dZ2_mean"])
+    n = float(n)
+    log_n, log_n1, log_n2 = math.log(n), math.log(n + 1.0), math.log(n + 2.0)
+    T_mean = LS(-_jnp_logaddexp(0.0, -log_n))
+    t_mean = LS(-log_n1)
+    T2_mean = LS(-_jnp_logaddexp(0.0, math.log(2.0) - log_n))
+    t2_mean = LS(math.log(2.0) - log_n1 - log_n2)
+    tT_mean = LS(-_jnp_logaddexp(0.0, -log_n) - log_n2)
+    dZ_mean = X_mean * t_mean * midL
+    next_X_mean = X_mean * T_mean
+    next_X2_mean = X2_mean * T2_mean
+    next_Z_mean = Z_mean + dZ_mean
+    next_ZX_mean = ZX_mean * T_mean + X2_mean * tT_mean * midL
+    next_Z2_mean = Z2_mean + LS(math.log(2.0)) * ZX_mean * t_mean * midL + (X2_mean * t2_mean * midL ** 2)
+    next_dZ2_mean = dZ2_mean + (X2_mean * t2_mean * midL ** 2)
+    return {"log_L": float(log_L_next), "log_X_mean": next_X_mean.v, "log_X2_mean": next_X2_mean.v,
+            "log_Z_mean": next_Z_mean.v, "log_Z2_mean": next_Z2_mean.v, "log_ZX_mean": next_ZX_mean.v,
+            "log_dZ_mean": dZ_mean.v, "log_dZ2_mean": next_dZ2_mean.v}
+
+
+def _restated_init():
+    """create_init_evidence_calc (shrinkage_statistics.py:112-128)."""
+    inf = float("inf")
+    return {"log_L": -inf, "log_X_mean": 0.0, "log_X2_mean": 0.0, "log_Z_mean": -inf, "log_ZX_mean": -inf,
+            "log_Z2_mean": -inf, "log_dZ_mean": -inf, "log_dZ2_mean": -inf}
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_restated_evidence_recurrence_is_bit_identical(oracle_mod, seed):
+    """Every per-sample field of compute_evidence_stats equals the restatement exactly, over
+    sample sets with a varying live-point count, ties and a -inf first likelihood."""
+    g = np.random.default_rng(seed)
+    M = 400
+    log_L = np.sort(np.round(g.standard_normal(M) * 5, 1))
+    if seed % 2:
+        log_L[0] = -np.inf
+    n = np.maximum(1, np.round(50 + 30 * np.sin(np.arange(M) / 17.0) - np.arange(M) / 20)).astype(np.float64)
+    fin, per = oracle_mod.compute_evidence_stats(log_L, n)
+    c = _restated_init()
+    for i in range(M):
+        c = _restated_update(c, n[i], log_L[i])
+        for f, v in c.items():
+            w = per[f][i]
+            assert (v == w) or (math.isnan(v) and math.isnan(w)), (i, f, v, w)
+    for f, v in c.items():
+        assert v == fin[f] or (math.isnan(v) and math.isnan(fin[f])), f
