@@ -1,6 +1,6 @@
-"""A second, independent restatement of the slice sampler's chain and of the FP64 evidence
-recurrence (plain Python, written from the reference's source, small cases only) against the C
-oracle on the same inputs.
+"""A second, independent restatement of the slice sampler's chain, the FP64 evidence
+recurrence and the results pass (plain Python, written from the reference's source, small cases
+only) against the C oracle on the same inputs.
 
 The C oracle is the checker for every GPU parity test, and jax cannot run here to pin it, so
 this test restates ``UniDimSliceSampler._get_sample`` once more, directly from
@@ -257,3 +257,72 @@ def test_restated_evidence_recurrence_is_bit_identical(oracle_mod, seed):
             assert (v == w) or (math.isnan(v) and math.isnan(w)), (i, f, v, w)
     for f, v in c.items():
         assert v == fin[f] or (math.isnan(v) and math.isnan(fin[f])), f
+
+
+# ------------------------------------------------------------------ _to_results
+
+def _logsumexp(a):
+    m = np.max(a)
+    if not np.isfinite(m):
+        return float(m)
+    return float(m + np.log(np.sum(np.exp(a - m))))
+
+
+def restated_to_results(o, run):
+    """ShardedStaticNestedSampler._to_results with trim=True (sharded_static.py:652-773) over
+    the run's stored samples: live-point counts, the evidence recurrence (restated above),
+    linear_to_log_stats (internals/stats.py:55-74), the phantom correction sqrt(1 + k), Kish's
+    ESS (stats.py:77-86), the normalised dp and H (instable form, stable fallback)."""
+    idx, nl = o.count_crossed_edges(run.sender, run.log_L)
+    log_L = run.log_L[idx]
+    c = _restated_init()
+    log_dZ, log_X = [], []
+    for i in range(len(log_L)):
+        c = _restated_update(c, nl[i], log_L[i])
+        log_dZ.append(c["log_dZ_mean"])
+        log_X.append(c["log_X_mean"])
+    log_dZ, log_X = np.array(log_dZ), np.array(log_X)
+    N = len(log_L)
+    log_Z_mean = 2.0 * c["log_Z_mean"] - 0.5 * c["log_Z2_mean"]
+    log_Z_var = max(c["log_Z2_mean"] - 2.0 * c["log_Z_mean"], np.finfo(np.float64).eps)
+    tp = int(np.sum(run.phantom != 0))
+    pf = tp / N
+    k = pf / (1.0 - pf)
+    log_Z_uncert = math.sqrt(log_Z_var) * math.sqrt(1.0 + k)
+    ESS = math.exp(2.0 * c["log_Z_mean"] - c["log_dZ2_mean"]) / (1.0 + k)
+    norm = _logsumexp(log_dZ)
+    log_dp = np.where(np.isneginf(norm), -np.inf, log_dZ - norm)
+    p = np.exp(log_dp)
+    H_instable = -(np.sum(p * np.where(np.isneginf(log_dp), 0.0, log_L)) - log_Z_mean)
+    H_stable = -np.sum(p * np.log(-log_X))
+    H = H_instable if np.isfinite(H_instable) else H_stable
+    total_evals = int(np.sum(run.nevals[idx]))
+    return {"log_Z_mean": log_Z_mean, "log_Z_uncert": log_Z_uncert, "ESS": ESS, "H_mean": H,
+            "total_num_samples": N, "total_phantom_samples": tp, "total_num_likelihood_evaluations": total_evals,
+            "log_efficiency": math.log(N) - math.log(total_evals), "log_dp_mean": log_dp, "log_X_mean": log_X,
+            "num_live_points": nl, "samples_indices": idx}
+
+
+@pytest.mark.parametrize("case", ["mvn", "shells_k2"])
+def test_restated_to_results(oracle_mod, case):
+    o = oracle_mod
+    if case == "mvn":
+        model = o.mvn_model(np.full(3, -10.0), np.full(3, 10.0), np.array([0.2, -0.1, 0.4]),
+                            np.array([[1.0, 0.3, 0.0], [0.3, 0.8, 0.2], [0.0, 0.2, 0.5]]))
+        run = o.ns_run(model, o.PRNGKey(21), num_live_points=60, num_slices=9, term_cond={"dlogZ": 1e-3})
+    else:
+        model = o.shells_model(-6.0, 6.0, [3.5, 0.0], [-3.5, 0.0], 2.0, 0.4)
+        run = o.ns_run(model, o.PRNGKey(22), num_live_points=50, num_slices=8, num_phantom=2,
+                       term_cond={"dlogZ": 1e-3})
+    want = restated_to_results(o, run)
+    got = run.results
+    for f in ("total_num_samples", "total_phantom_samples", "total_num_likelihood_evaluations"):
+        assert int(got[f]) == want[f], f
+    for f in ("log_Z_mean", "log_Z_uncert", "ESS", "H_mean", "log_efficiency"):
+        np.testing.assert_allclose(got[f], want[f], rtol=1e-10, atol=1e-12, err_msg=f)
+    np.testing.assert_array_equal(run.samples_indices, want["samples_indices"])
+    np.testing.assert_array_equal(run.num_live_points, want["num_live_points"])
+    np.testing.assert_array_equal(run.log_X_mean, want["log_X_mean"])
+    np.testing.assert_allclose(run.log_dp_mean, want["log_dp_mean"], rtol=1e-12, atol=1e-12)
+    if case == "shells_k2":
+        assert want["total_phantom_samples"] > 0
