@@ -39,6 +39,8 @@ def test_items_cover_every_chain_once_and_buckets_are_contiguous():
             lo, hi = b._b.bucket_begin[k], b._b.bucket_end[k]
             for r, *_ in items[lo:hi]:
                 assert specs[r].family * 4 + _dbucket(specs[r].D) == k
+            Ds = [specs[r].D for r, *_ in items[lo:hi]]
+            assert Ds == sorted(Ds, reverse=True)     # longest (largest D) first in a bucket
         assert sum(b._b.bucket_end[k] - b._b.bucket_begin[k] for k in range(8)) == len(items)
 
 
