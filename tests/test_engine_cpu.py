@@ -13,7 +13,8 @@ def _specs():
     out = []
     rng = np.random.default_rng(0)
     for i, (fam, D, n) in enumerate([(FAMILY_MVN, 4, 64), (FAMILY_MVN, 12, 200), (FAMILY_MVN, 20, 96),
-                                     (FAMILY_MVN, 40, 128), (FAMILY_SHELLS, 6, 80), (FAMILY_SHELLS, 50, 100)]):
+                                     (FAMILY_MVN, 40, 128), (FAMILY_SHELLS, 6, 80), (FAMILY_SHELLS, 50, 100),
+                                     (FAMILY_MVN, 9, 60), (FAMILY_MVN, 14, 90)]):
         s = n // 2
         out.append(RunSpec(D=D, num_live_points=n, shell_size=s, num_slices=2 * D, family=fam,
                            params=rng.standard_normal(D * D + 3 * D + 3).astype(np.float32),
