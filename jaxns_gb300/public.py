@@ -294,6 +294,10 @@ class NestedSampler:
             init_efficiency_threshold=self.init_efficiency_threshold, shell_fraction=self.shell_fraction,
             devices=self.devices, verbose=self.verbose, store_U=self.store_U)
         self.num_live_points = self._nested_sampler.num_live_points
+        # post-analysis utilities attached as in the reference (summary and plotting are not built)
+        from .utils import load_results, save_results
+        self.save_results = save_results
+        self.load_results = load_results
 
     @property
     def nested_sampler(self) -> ShardedStaticNestedSampler:

@@ -1,0 +1,49 @@
+"""NestedSampler's defaults and validation (public.py:69-137), host logic only: no kernel runs
+until the sampler is called."""
+import numpy as np
+import pytest
+
+gb = pytest.importorskip("jaxns_gb300")
+
+
+def _model(D=3):
+    def prior_model():
+        x = yield gb.Prior(gb.Uniform(-10 * np.ones(D), 10 * np.ones(D)), name="x")
+        return x
+    return gb.Model(prior_model, gb.MultivariateNormalLikelihood(np.zeros(D), np.eye(D)))
+
+
+def test_defaults():
+    ns = gb.NestedSampler(_model(3))
+    assert (ns.s, ns.num_slices, ns.k, ns.c, ns.max_samples) == (5, 15, 0, 90, 9000)
+    assert ns.nested_sampler.sampler.midpoint_shrink and ns.nested_sampler.sampler.num_phantom_save == 0
+
+
+def test_difficult_model():
+    ns = gb.NestedSampler(_model(3), difficult_model=True)
+    assert (ns.s, ns.num_slices, ns.c, ns.max_samples) == (10, 30, 300, 30000)
+    assert not ns.nested_sampler.sampler.midpoint_shrink
+
+
+def test_parameter_estimation_phantoms():
+    ns = gb.NestedSampler(_model(3), parameter_estimation=True, num_live_points=100)
+    # k = min(D, s D - 1) phantoms; c = num_live_points / (k + 1) chains; 100 shrinkages
+    assert (ns.k, ns.c, ns.max_samples) == (3, 25, 25 * 4 * 100)
+    assert ns.nested_sampler.sampler.num_phantom_save == 3
+
+
+def test_explicit_values_and_gradient_guided():
+    ns = gb.NestedSampler(_model(4), num_slices=7, num_live_points=64, max_samples=1234, gradient_guided=True)
+    assert (ns.num_slices, ns.k, ns.c, ns.max_samples) == (7, 0, 64, 1234)
+    assert ns.nested_sampler.sampler.gradient_guided
+
+
+@pytest.mark.parametrize("kw", [{"s": 0}, {"k": 15}, {"k": -1}, {"c": 0}])
+def test_invalid_arguments_raise(kw):
+    with pytest.raises(ValueError):
+        gb.NestedSampler(_model(3), **kw)
+
+
+def test_post_analysis_utilities_attached():
+    ns = gb.NestedSampler(_model(2))
+    assert ns.save_results is gb.save_results and ns.load_results is gb.load_results
