@@ -147,3 +147,23 @@ def test_set_live_writes_the_run_slice():
     for q in range(len(specs)):      # the other runs' slices are untouched
         if q != r:
             assert not b.live_view(q)["log_L"].any()
+
+
+def test_shrinkage_coefficient_table():
+    """ncoef_table rows are the n-only terms of _update_evidence_calc_op
+    (internals/shrinkage_statistics.py:55-73): log T, log t, log T2, log t2, log tT."""
+    import math
+    from jaxns_gb300.engine import ncoef_table
+
+    def lae(a, b):
+        return max(a, b) + math.log1p(math.exp(-abs(a - b)))
+
+    tab = ncoef_table(300)
+    assert tab.shape == (301, 8)
+    for n in (1, 2, 3, 7, 50, 299, 300):
+        ln, ln1, ln2 = math.log(n), math.log(n + 1), math.log(n + 2)
+        want = [-lae(0.0, -ln), -ln1, -lae(0.0, math.log(2.0) - ln), math.log(2.0) - ln1 - ln2, -lae(0.0, -ln) - ln2]
+        np.testing.assert_allclose(tab[n, :5], want, rtol=1e-14, atol=1e-15)
+        # and they are the logs of n/(n+1), 1/(n+1), n/(n+2), 2/((n+1)(n+2)), n/((n+1)(n+2))
+        np.testing.assert_allclose(np.exp(tab[n, :5]), [n / (n + 1), 1 / (n + 1), n / (n + 2),
+                                                        2 / ((n + 1) * (n + 2)), n / ((n + 1) * (n + 2))], rtol=1e-13)
