@@ -107,6 +107,45 @@ def _dbucket(D: int) -> int:
     raise ValueError(f"D={D} > 64 is not supported by the fused slice kernel")
 
 
+def param_count(family: int, D: int, N: int = 0) -> int:
+    """Length of a run's parameter vector: MVN [mu, Linv, c0], shells [c1, c2, R, w, norm],
+    linear-Gaussian [Phi (N x P row-major), y, sigma]."""
+    if family == FAMILY_MVN:
+        return D + D * D + 1
+    if family == FAMILY_SHELLS:
+        return 2 * D + 3
+    if family == FAMILY_LINGAUSS:
+        return N * D + N + 1
+    raise ValueError(f"unknown likelihood family {family}")
+
+
+def validate_spec(s: RunSpec, r: int = 0) -> None:
+    """Reject a run the kernels would index out of bounds with (every size they read from the
+    run descriptor is checked here, on the host)."""
+    where = f"run {r}"
+    if not 1 <= s.D <= 64:
+        raise ValueError(f"{where}: D={s.D} outside [1, 64]")
+    if not 1 <= s.shell_size <= s.num_live_points:
+        raise ValueError(f"{where}: shell size {s.shell_size} outside [1, num_live_points={s.num_live_points}]")
+    if s.num_slices < 1 or not 0 <= s.num_phantom < s.num_slices:
+        raise ValueError(f"{where}: need num_slices >= 1 and 0 <= num_phantom < num_slices "
+                         f"(got {s.num_slices}, {s.num_phantom})")
+    if s.max_samples < 1:
+        raise ValueError(f"{where}: max_samples must be positive")
+    if s.family == FAMILY_LINGAUSS and s.N < 1:
+        raise ValueError(f"{where}: the linear-Gaussian family needs N >= 1 data rows")
+    need = param_count(s.family, s.D, s.N)
+    if len(s.params) != need:
+        raise ValueError(f"{where}: family {s.family} with D={s.D} takes {need} parameters, got {len(s.params)}")
+    for name in ("prior_kind", "prior_a", "prior_b"):
+        if len(getattr(s, name)) != s.D:
+            raise ValueError(f"{where}: {name} must have D={s.D} entries")
+    if not np.all(np.isin(np.asarray(s.prior_kind), (PRIOR_UNIFORM, PRIOR_NORMAL))):
+        raise ValueError(f"{where}: prior kinds are {PRIOR_UNIFORM} (Uniform) or {PRIOR_NORMAL} (Normal)")
+    if np.shape(s.key) != (2,):
+        raise ValueError(f"{where}: key must be two uint32 words")
+
+
 def _ptr(t: Optional[torch.Tensor]) -> Optional[int]:
     return None if t is None else t.data_ptr()
 
@@ -146,8 +185,8 @@ class NSBatch:
         self.gradient_guided = gg.pop()
         if self.gradient_guided and any(s.family == FAMILY_LINGAUSS for s in specs):
             raise NotImplementedError("the gradient-guided slice is not on the linear-Gaussian lock step")
-        for s in specs:
-            _dbucket(s.D)
+        for r, s in enumerate(specs):
+            validate_spec(s, r)
         live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])
         store_off = np.concatenate([[0], np.cumsum(caps)[:-1]])
         shell_off = np.concatenate([[0], np.cumsum(ss)[:-1]])

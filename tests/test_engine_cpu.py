@@ -17,7 +17,7 @@ def _specs():
                                      (FAMILY_MVN, 9, 60), (FAMILY_MVN, 14, 90)]):
         s = n // 2
         out.append(RunSpec(D=D, num_live_points=n, shell_size=s, num_slices=2 * D, family=fam,
-                           params=rng.standard_normal(D * D + 3 * D + 3).astype(np.float32),
+                           params=rng.standard_normal(D + D * D + 1 if fam == FAMILY_MVN else 2 * D + 3).astype(np.float32),
                            prior_kind=np.zeros(D, np.int32), prior_a=np.zeros(D), prior_b=np.ones(D),
                            max_samples=10 * n, term_cond={"dlogZ": 1e-4, "max_samples": 10.0 * n},
                            key=np.array([0, i], np.uint32), store_U=(i % 2 == 0)))
@@ -167,3 +167,26 @@ def test_shrinkage_coefficient_table():
         # and they are the logs of n/(n+1), 1/(n+1), n/(n+2), 2/((n+1)(n+2)), n/((n+1)(n+2))
         np.testing.assert_allclose(np.exp(tab[n, :5]), [n / (n + 1), 1 / (n + 1), n / (n + 2),
                                                         2 / ((n + 1) * (n + 2)), n / ((n + 1) * (n + 2))], rtol=1e-13)
+
+
+@pytest.mark.parametrize("change,match", [
+    ({"shell_size": 0}, "shell size"), ({"shell_size": 65}, "shell size"), ({"num_slices": 0}, "num_slices"),
+    ({"num_phantom": 8}, "num_phantom"), ({"max_samples": 0}, "max_samples"), ({"D": 65}, "D=65"),
+    ({"params": np.zeros(5, np.float32)}, "parameters"), ({"prior_a": np.zeros(3)}, "prior_a"),
+    ({"prior_kind": np.full(4, 7, np.int32)}, "prior kinds"), ({"key": np.zeros(3, np.uint32)}, "key")])
+def test_malformed_runs_are_rejected_on_the_host(change, match):
+    """Every size a kernel reads from the run descriptor is checked before any buffer exists."""
+    import dataclasses
+    from jaxns_gb300.engine import NSBatch
+    spec = dataclasses.replace(_specs()[0], **change)    # MVN, D = 4, n = 64, s = 32, S = 8
+    with pytest.raises(ValueError, match=match):
+        NSBatch([spec], device="cpu")
+
+
+def test_lingauss_needs_data_rows():
+    import dataclasses
+    from jaxns_gb300.engine import FAMILY_LINGAUSS, NSBatch, param_count
+    spec = dataclasses.replace(_specs()[0], family=FAMILY_LINGAUSS, N=0, params=np.zeros(1, np.float32))
+    with pytest.raises(ValueError, match="N >= 1"):
+        NSBatch([spec], device="cpu", lg_tensor_cores=False)
+    assert param_count(FAMILY_LINGAUSS, 4, 10) == 51
