@@ -61,6 +61,40 @@ def _run_summary(o, run) -> dict:
     }
 
 
+def tree_inputs():
+    """A seeded 200-sample tree with ties on a quarter grid: (sender node index, log L).  Every
+    sender has a strictly lower log L; storage order shuffled; the sender is a node index, 0 the
+    root and sample i node i + 1, as in SampleTreeGraph (internals/tree_structure.py:12-26)."""
+    g = np.random.default_rng(11)
+    N = 200
+    asc = np.round(np.sort(g.standard_normal(N)) * 4) / 4
+    parent = np.full(N, -1, np.int64)
+    for i in range(N):
+        lower = np.flatnonzero(asc < asc[i])
+        if lower.size and g.random() < 0.9:
+            parent[i] = int(lower[g.integers(max(0, lower.size - 30), lower.size)])
+    perm = g.permutation(N)                 # storage slot of the i-th ascending sample
+    log_L = np.empty(N)
+    sender = np.empty(N, np.int64)
+    log_L[perm] = asc
+    sender[perm] = np.where(parent >= 0, perm[np.maximum(parent, 0)] + 1, 0)
+    return sender, log_L
+
+
+def evidence_inputs():
+    """A seeded sample set for compute_evidence_stats: (sorted log L [500], live-point counts)."""
+    g = np.random.default_rng(12)
+    M = 500
+    ll = np.sort(g.standard_normal(M)) * 3
+    n = np.concatenate([np.full(M - 40, 40), np.arange(40, 0, -1)]).astype(np.float64)
+    return ll, n
+
+
+# the small complete run both fixture generators record (correlated Gaussian, D = 2)
+MVN_RUN = {"mu": [0.3, -0.4], "cov": [[1.0, 0.4], [0.4, 0.6]], "low": -10.0, "high": 10.0,
+           "num_live_points": 60, "num_slices": 10, "key_seed": 7, "dlogZ": 1e-3}
+
+
 def generate() -> dict:
     from oracle import oracle as o
     o.build()
@@ -81,38 +115,21 @@ def generate() -> dict:
     out["rng"] = rng
 
     # live-point count of a seeded tree with ties (tree_structure.py:33-108)
-    # (a valid tree: every sender has a strictly lower log L; storage order shuffled; the sender
-    # is a node index, 0 the root and sample i node i + 1, as in SampleTreeGraph)
-    g = np.random.default_rng(11)
-    N = 200
-    asc = np.round(np.sort(g.standard_normal(N)) * 4) / 4   # ties on a quarter grid
-    parent = np.full(N, -1, np.int64)
-    for i in range(N):
-        lower = np.flatnonzero(asc < asc[i])
-        if lower.size and g.random() < 0.9:
-            parent[i] = int(lower[g.integers(max(0, lower.size - 30), lower.size)])
-    perm = g.permutation(N)                 # storage slot of the i-th ascending sample
-    log_L = np.empty(N)
-    sender = np.empty(N, np.int64)
-    log_L[perm] = asc
-    sender[perm] = np.where(parent >= 0, perm[np.maximum(parent, 0)] + 1, 0)
+    sender, log_L = tree_inputs()
     idx, nl = o.count_crossed_edges(sender, log_L)
-    out["tree"] = {"sender_seed": 11, "N": N, "samples_indices": [int(v) for v in idx],
+    out["tree"] = {"sender_seed": 11, "N": len(log_L), "samples_indices": [int(v) for v in idx],
                    "num_live_points": [int(v) for v in nl]}
 
     # FP64 evidence statistics (shrinkage_statistics.py:131-157)
-    g = np.random.default_rng(12)
-    M = 500
-    ll = np.sort(g.standard_normal(M)) * 3
-    n = np.concatenate([np.full(M - 40, 40), np.arange(40, 0, -1)]).astype(np.float64)
+    ll, n = evidence_inputs()
     fin, _ = o.compute_evidence_stats(ll, n)
-    out["evidence_stats"] = {"seed": 12, "M": M, "final": {k: _f(v) for k, v in fin.items()}}
+    out["evidence_stats"] = {"seed": 12, "M": len(ll), "final": {k: _f(v) for k, v in fin.items()}}
 
     # a complete MVN run (D = 2) and a shells run with phantoms (D = 3, k = 2)
-    mu = np.array([0.3, -0.4])
-    cov = np.array([[1.0, 0.4], [0.4, 0.6]])
-    m1 = o.mvn_model(np.full(2, -10.0), np.full(2, 10.0), mu, cov)
-    r1 = o.ns_run(m1, o.PRNGKey(7), num_live_points=60, num_slices=10, term_cond={"dlogZ": 1e-3})
+    c = MVN_RUN
+    m1 = o.mvn_model(np.full(2, c["low"]), np.full(2, c["high"]), np.array(c["mu"]), np.array(c["cov"]))
+    r1 = o.ns_run(m1, o.PRNGKey(c["key_seed"]), num_live_points=c["num_live_points"], num_slices=c["num_slices"],
+                  term_cond={"dlogZ": c["dlogZ"]})
     m2 = o.shells_model(-6.0, 6.0, [3.5, 0.0, 0.0], [-3.5, 0.0, 0.0], 2.0, 0.3)
     r2 = o.ns_run(m2, o.PRNGKey(8), num_live_points=80, num_slices=15, num_phantom=2,
                   term_cond={"dlogZ": 1e-3})
