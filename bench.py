@@ -47,6 +47,29 @@ METRIC = "NS runs/s & likelihood evals/s at |dlogZ|<0.1, batched/adjoint vs plai
 SHELLS_D = 10
 
 
+REQUIRED = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+            "vs_baseline", "dtype", "data", "config", "gpu_launches", "roofline", "clocks")
+REQUIRED_SUB = {"roofline": ("bound", "achieved", "peak", "unit", "frac", "traffic"),
+                "e2e": ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"),
+                "cpu_baseline": ("value", "unit", "cores", "kind", "sample"),
+                "clocks": ("sm_mhz", "sm_max_mhz", "reasons")}
+
+
+def check_line(line: dict, e2e: bool = True, cpu: bool = True) -> dict:
+    """Raise unless the result line carries every key of the benchmark contract (e2e and
+    cpu_baseline unless they were switched off on the command line)."""
+    need = list(REQUIRED) + (["e2e"] if e2e else []) + (["cpu_baseline"] if cpu else [])
+    missing = [k for k in need if k not in line or (k in REQUIRED_SUB and line[k] is None)]
+    for k in need:
+        if k in REQUIRED_SUB and isinstance(line.get(k), dict):
+            missing += [f"{k}.{sub}" for sub in REQUIRED_SUB[k] if sub not in line[k]]
+    if not isinstance(line.get("config"), dict) or "workload" not in line["config"]:
+        missing.append("config.workload")
+    if missing:
+        raise RuntimeError(f"result line lacks {missing}")
+    return line
+
+
 def workload(R: int, seed: int = 2024, name: str = "shells"):
     """Seeded problems: list of (D, kind, params, n, S, cap)."""
     out = []
@@ -423,7 +446,7 @@ def main():
         line["cpu_baseline"] = {"value": v, "unit": "runs/s", "cores": threads, "kind": "port",
                                 "sample": info["sample"]}
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(check_line(line, e2e=True, cpu=not args.no_cpu)))
     if world > 1:
         torch.distributed.destroy_process_group()
 
@@ -739,7 +762,7 @@ def main_blr(args):
                                           f"problems {idx}, x each problem's evaluation count in this run, "
                                           f"spread over {threads} host threads (NS overhead and adjoint excluded)"}
     if rank == 0:
-        print(json.dumps(line))
+        print(json.dumps(check_line(line, e2e=not args.no_e2e, cpu=not args.no_cpu)))
     if world > 1:
         torch.distributed.destroy_process_group()
 
