@@ -11,6 +11,9 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and libgbns.so")
+    # temporary files of the tests stay inside the repository, in the git-ignored build folder
+    if not config.option.basetemp:
+        config.option.basetemp = os.path.join(ROOT, "_build", "pytest-tmp")
 
 
 def corr_gauss(D, seed):

@@ -158,3 +158,21 @@ def test_integration_ctypes_stub_runs(lib):
     assert b"NULL" in stub_lib.gbns_last_error()
     assert stub_lib.gbns_evidence_adjoint_tc(None, None, 0, 0, None, None, 0, 0.0, 0.0, None, None, None, None,
                                              None, None, None) == -1
+
+
+def test_header_and_library_from_plain_c(lib, tmp_path):
+    """include/gbns.h compiles as C (gcc -std=c99) and the C program links and runs against the
+    built library: sizes seen by a C compiler equal the library's own."""
+    import shutil
+    import subprocess
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no gcc")
+    libdir = os.path.dirname(lib._name)
+    exe = str(tmp_path / "abi_from_c")
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "abi_from_c.c"), "-L", libdir, "-lgbns",
+                    f"-Wl,-rpath,{libdir}", "-o", exe], check=True, capture_output=True, text=True)
+    out = subprocess.run([exe], capture_output=True, text=True, timeout=60)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    assert out.stdout.startswith("ok 1 ")
