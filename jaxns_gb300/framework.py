@@ -138,16 +138,19 @@ class Model:
         return X if is_t else X.numpy()
 
     def log_prob_prior(self, U):
-        """log prior density of the X that U maps to (per sample)."""
+        """log prior density of the X that U maps to (per sample); a tensor for a tensor U, a
+        numpy array otherwise."""
         import torch
-        X = self.transform_flat(U)
+        is_t = isinstance(U, torch.Tensor)
+        X = self.transform_flat(U if is_t else torch.as_tensor(np.asarray(U, np.float64)))
         a = torch.as_tensor(self.prior_a, dtype=X.dtype, device=X.device)
         b = torch.as_tensor(self.prior_b, dtype=X.dtype, device=X.device)
         normal = torch.as_tensor(self.prior_kind == PRIOR_NORMAL, device=X.device)
         inside = (X >= a) & (X <= a + b)
         lp_u = torch.where(inside, -torch.log(b), torch.full_like(X, -float("inf")))
         lp_n = -0.5 * ((X - a) / b) ** 2 - torch.log(b) - 0.5 * np.log(2.0 * np.pi)
-        return torch.where(normal, lp_n, lp_u).sum(-1)
+        lp = torch.where(normal, lp_n, lp_u).sum(-1)
+        return lp if is_t else lp.numpy()
 
     @property
     def U_placeholder(self):
