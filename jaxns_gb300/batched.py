@@ -19,7 +19,7 @@ from .public import NestedSampler, NestedSamplerResults, TerminationCondition, r
 class BatchedNestedSampler:
     def __init__(self, samplers: Sequence[NestedSampler], keys, term_conds: Optional[Sequence] = None,
                  block: int = 16, chains_per_item: int = 64, store_U: bool = False, lg_tensor_cores: bool = True,
-                 autotune: bool = False, wide_chains_per_item: int = 0):
+                 autotune: bool = False, wide_chains_per_item: int = 0, device="cuda"):
         self.samplers = list(samplers)
         keys = np.asarray(keys, np.uint32).reshape(len(self.samplers), 2)
         if term_conds is None:
@@ -37,8 +37,8 @@ class BatchedNestedSampler:
             self.tuning = autotune_launch(specs)
             chains_per_item = self.tuning["chains_per_item"]
             wide_chains_per_item = self.tuning["wide_chains_per_item"]
-        self.batch = NSBatch(specs, chains_per_item=chains_per_item, wide_chains_per_item=wide_chains_per_item,
-                             lg_tensor_cores=lg_tensor_cores)
+        self.batch = NSBatch(specs, device=device, chains_per_item=chains_per_item,
+                             wide_chains_per_item=wide_chains_per_item, lg_tensor_cores=lg_tensor_cores)
         self.state = None
 
     def __call__(self, from_host: bool = True, use_graph: bool = True, check: bool = True,

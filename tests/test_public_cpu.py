@@ -47,3 +47,22 @@ def test_invalid_arguments_raise(kw):
 def test_post_analysis_utilities_attached():
     ns = gb.NestedSampler(_model(2))
     assert ns.save_results is gb.save_results and ns.load_results is gb.load_results
+
+
+def test_batched_sampler_assembles_one_run_per_problem():
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.batched import BatchedNestedSampler
+    samplers = [gb.NestedSampler(_model(D), num_live_points=20 * D) for D in (2, 5, 3)]
+    keys = np.array([[0, 7], [1, 8], [2, 9]], np.uint32)
+    tcs = [None, gb.TerminationCondition(dlogZ=0.5), gb.TerminationCondition(max_samples=500)]
+    b = BatchedNestedSampler(samplers, keys, tcs, store_U=False, device="cpu")
+    specs = b.batch.specs
+    assert [s.D for s in specs] == [2, 5, 3] and [s.num_live_points for s in specs] == [40, 100, 60]
+    for s, k in zip(specs, keys):
+        np.testing.assert_array_equal(s.key, k)
+        assert not s.store_U
+    assert specs[0].term_cond["dlogZ"] == pytest.approx(np.log(1 + 1e-3))     # the default condition
+    assert specs[1].term_cond["dlogZ"] == 0.5
+    assert specs[2].term_cond["max_samples"] == 500                            # min(500, the sampler's cap)
+    with pytest.raises(_ffi.GBNSError, match="no CPU path"):
+        b()
