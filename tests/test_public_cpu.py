@@ -66,3 +66,34 @@ def test_batched_sampler_assembles_one_run_per_problem():
     assert specs[2].term_cond["max_samples"] == 500                            # min(500, the sampler's cap)
     with pytest.raises(_ffi.GBNSError, match="no CPU path"):
         b()
+
+
+@pytest.mark.parametrize("kw,exc", [({"num_slices": 0}, ValueError), ({"num_phantom_save": -1}, ValueError),
+                                    ({"num_phantom_save": 5}, ValueError), ({"perfect": False}, ValueError),
+                                    ({"adaptive_shrink": True}, NotImplementedError),
+                                    ({"gradient_slice": True}, NotImplementedError)])
+def test_slice_sampler_validation(kw, exc):
+    """samplers/uni_slice_sampler.py:276-326."""
+    from jaxns_gb300.public import UniDimSliceSampler
+    args = dict(model=_model(2), num_slices=5, num_phantom_save=0, midpoint_shrink=True, perfect=True)
+    args.update(kw)
+    with pytest.raises(exc):
+        UniDimSliceSampler(**args)
+
+
+def test_static_sampler_rounding():
+    """sharded_static.py:577-594, :625-650: shell fraction at least 1/n, store capacity a
+    multiple of one shell with its phantoms."""
+    from jaxns_gb300.public import ShardedStaticNestedSampler, UniDimSliceSampler
+    m = _model(2)
+    sl = UniDimSliceSampler(model=m, num_slices=6, num_phantom_save=2, midpoint_shrink=True, perfect=True)
+    ss = ShardedStaticNestedSampler(model=m, max_samples=1001, init_efficiency_threshold=0.1, sampler=sl,
+                                    num_live_points=50)
+    assert ss.shell_fraction == 0.5 and ss.num_live_points == 50
+    assert ss.max_samples == 1050          # 25 discards x (1 + 2 phantoms) = 75 per shell
+    one = ShardedStaticNestedSampler(model=m, max_samples=10, init_efficiency_threshold=0.1, sampler=sl,
+                                     num_live_points=4, shell_fraction=0.1)
+    assert one.shell_fraction == 0.25      # at least one discard per shell
+    with pytest.raises(ValueError):
+        ShardedStaticNestedSampler(model=m, max_samples=10, init_efficiency_threshold=0.1, sampler=sl,
+                                   num_live_points=4, shell_fraction=1.5)
