@@ -97,3 +97,29 @@ def test_static_sampler_rounding():
     with pytest.raises(ValueError):
         ShardedStaticNestedSampler(model=m, max_samples=10, init_efficiency_threshold=0.1, sampler=sl,
                                    num_live_points=4, shell_fraction=1.5)
+
+
+def test_termination_condition_fields_and_struct():
+    """Every field of TerminationCondition reaches the device struct with its has_ flag."""
+    from jaxns_gb300.engine import term_cond_struct
+    from jaxns_gb300.public import TerminationConditionConjunction, TerminationConditionDisjunction
+    tc = gb.TerminationCondition(ess=100, evidence_uncert=0.1, dlogZ=0.01, max_samples=1e4,
+                                 max_num_likelihood_evaluations=1e6, log_L_contour=-3.0, efficiency_threshold=0.05,
+                                 rtol=1e-3, atol=1e-4, peak_XL_frac=0.2)
+    s = term_cond_struct(tc.as_dict())
+    for flag, field, v in [("has_ess", "ess", 100), ("has_evidence_uncert", "evidence_uncert", 0.1),
+                           ("has_dlogZ", "dlogZ", 0.01), ("has_max_samples", "max_samples", 1e4),
+                           ("has_max_nlik", "max_nlik", 1e6), ("has_log_L_contour", "log_L_contour", -3.0),
+                           ("has_efficiency", "efficiency_threshold", 0.05), ("has_rtol", "rtol", 1e-3),
+                           ("has_atol", "atol", 1e-4), ("has_peak_XL", "peak_XL_frac", 0.2)]:
+        assert getattr(s, flag) == 1 and getattr(s, field) == pytest.approx(v), field
+    empty = term_cond_struct(gb.TerminationCondition().as_dict())
+    assert empty.has_dlogZ == 0 and empty.has_max_samples == 0
+    with pytest.warns(UserWarning):
+        assert "live_evidence_frac" not in gb.TerminationCondition(live_evidence_frac=0.1).as_dict()
+    assert isinstance(tc & tc, TerminationConditionConjunction) and isinstance(tc | tc, TerminationConditionDisjunction)
+    ns = gb.NestedSampler(_model(2))
+    with pytest.raises(TypeError):
+        ns.normalise_term_cond(tc | tc)
+    norm = ns.normalise_term_cond(gb.TerminationCondition(dlogZ=0.1))
+    assert norm.max_samples == ns.nested_sampler.max_samples and norm.dlogZ == 0.1
