@@ -13,8 +13,10 @@
  *   - threefry2x32_20 is checked against the Random123 known-answer vectors (tests).
  *   - count_crossed_edges / cumulative ops against the reference's own unit-test values.
  *   - the key-derivation layout (jax_threefry_partitionable=True) and XLA's f64 erfinv
- *     cannot be checked here (no JAX in this environment): "parity unpinned" for those.
+ *     cannot be checked here (no JAX in this environment): "parity unpinned" for those;
+ *     tests/golden/make_jax_golden.py records jax's outputs where jax is installed.
  */
+#define _POSIX_C_SOURCE 199309L /* clock_gettime under strict C modes as well */
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
