@@ -246,3 +246,42 @@ def test_gradient_guided_log_Z(gpu_lib):
     res = ns.to_results(reason, state)
     assert abs(res.log_Z_mean + D * np.log(20.0)) < 4 * res.log_Z_uncert + 0.02, (res.log_Z_mean, res.log_Z_uncert)
     assert res.total_num_likelihood_evaluations > 0
+
+
+def test_empty_and_single_sample_sets(gpu_lib, oracle_mod):
+    """The empty and one-sample edge cases the reference's own tests exercise: tree count,
+    FP64 evidence statistics and sample_evidence with N = 0 and N = 1 against the oracle
+    (device buffers keep one element so that no pointer is NULL)."""
+    from jaxns_gb300 import _ffi, sample_evidence
+    from jaxns_gb300.engine import ncoef_table
+    tab = torch.tensor(ncoef_table(64), device="cuda")
+    for N in (0, 1):
+        n1 = max(N, 1)
+        ts = torch.zeros(n1, dtype=torch.int32, device="cuda")          # the one sample hangs off the root
+        tL = torch.full((n1,), -2.0, dtype=torch.float32, device="cuda")
+        si = torch.full((n1,), -7, dtype=torch.int32, device="cuda")
+        nl = torch.full((n1,), -7, dtype=torch.int32, device="cuda")
+        sll = torch.zeros(2 * (N + 1), dtype=torch.int64, device="cuda")
+        si_ = torch.zeros(N + 1, dtype=torch.int32, device="cuda")
+        _ffi.call("gbns_count_crossed_edges", _p(ts), _p(tL), ctypes.c_longlong(N), _p(si), _p(nl), _p(sll), _p(si_),
+                  _s())
+        osi, onl = oracle_mod.count_crossed_edges(np.zeros(N, np.int64), np.full(N, -2.0))
+        np.testing.assert_array_equal(si.cpu().numpy()[:N], osi)
+        np.testing.assert_array_equal(nl.cpu().numpy()[:N], onl)
+
+        tn = torch.full((n1,), 3, dtype=torch.int32, device="cuda")
+        fin = torch.zeros(8, dtype=torch.float64, device="cuda")
+        lX, ldZ, lZ = (torch.zeros(n1, dtype=torch.float64, device="cuda") for _ in range(3))
+        _ffi.call("gbns_evidence_stats", _p(tL), _p(tn), ctypes.c_longlong(N), _p(tab), ctypes.c_int(64), _p(fin),
+                  _p(lX), _p(ldZ), _p(lZ), _s())
+        ofin, _ = oracle_mod.compute_evidence_stats(np.full(N, -2.0), np.full(N, 3.0))
+        names = ("log_L", "log_X_mean", "log_X2_mean", "log_Z_mean", "log_ZX_mean", "log_Z2_mean", "log_dZ_mean",
+                 "log_dZ2_mean")
+        np.testing.assert_allclose(fin.cpu().numpy(), [ofin[k] for k in names], rtol=1e-6, atol=1e-6)
+
+        key = oracle_mod.PRNGKey(1)
+        got = sample_evidence(key, np.full(N, 5, np.int64), np.full(N, -1.0), S=3).cpu().numpy()
+        ref = oracle_mod.sample_evidence(key, np.full(N, 5, np.int64), np.full(N, -1.0), S=3)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-9)
+        if N == 0:
+            assert np.all(np.isneginf(got))
