@@ -13,6 +13,7 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and libgbns.so")
     # temporary files of the tests stay inside the repository, in the git-ignored build folder
     if not config.option.basetemp:
+        os.makedirs(os.path.join(ROOT, "_build"), exist_ok=True)   # pytest creates only the last level
         config.option.basetemp = os.path.join(ROOT, "_build", "pytest-tmp")
 
 
