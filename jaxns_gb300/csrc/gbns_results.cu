@@ -130,6 +130,8 @@ __device__ void cta_count_edges(const int *sender, long long N, const unsigned l
   }
 }
 
+// count_crossed_edges (internals/tree_structure.py:33-108) of one sample set on one CTA:
+// stable sort of the N+1 nodes, out-degrees, crossed-edge scan (gbns_count_crossed_edges).
 __global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const float *L, long long N,
                                                       int *samples_indices, int *num_live,
                                                       unsigned long long *scratch, int *deg) {
@@ -138,6 +140,8 @@ __global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const f
   cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm);
 }
 
+// compute_evidence_stats (internals/shrinkage_statistics.py:131-157) of one sample set on one
+// warp: the final register and the per-sample log X, log dZ and log Z, FP64 (gbns_evidence_stats).
 __global__ void k_evidence_stats(const float *L, const int *nl, long long N, const double *ncoef, int nmax,
                                  gbns_evcalc *fin, double *lX, double *ldZ, double *lZ) {
   gbns_evcalc e;
@@ -150,6 +154,9 @@ __global__ void k_evidence_stats(const float *L, const int *nl, long long N, con
 
 // ------------------------------------------------------------ results ----
 
+// _to_results (sharded_static.py:652-773) for every run of a batch, one CTA per run: tree count
+// of the run's store, gather in sorted order, FP64 evidence per sample, log Z mean and
+// uncertainty with the phantom correction, ESS, H, efficiency.
 __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_bufs res) {
   __shared__ RadixSmem sm;
   __shared__ double dred[32];
@@ -249,6 +256,8 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
 
 // ---------------------------------------------------------- RNG hooks ----
 
+// jax.random under jax_threefry_partitionable (set by internals/mixed_precision.py:11), for the
+// parity tests: mode 0 raw threefry2x32 words, 1 split, 2 64-bit words, 3 uniform, 4 normal.
 __global__ void k_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= n) return;
