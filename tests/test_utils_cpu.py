@@ -103,3 +103,29 @@ def test_trim_results_cuts_per_sample_arrays():
     assert (t.log_Z_mean, t.total_num_samples, t.termination_reason) == (-1.5, N, 4)
     one = res._replace(log_dp_mean=np.zeros(1))
     assert NestedSampler.trim_results(one).log_dp_mean.shape == (1,)
+
+
+def test_dead_set_log_weights():
+    """DeadSet.from_results: log w_i = log dp_i - log L_i + log Z (experimental/
+    evidence_maximisation.py:213), so at the run's own hyperparameters the reweighted evidence
+    logsumexp_i(log L_i + log w_i) is log Z again (the normalised dp sum to one)."""
+    torch = pytest.importorskip("torch")
+    from scipy.special import logsumexp
+    from jaxns_gb300.adjoint import DeadSet
+    from jaxns_gb300.public import NestedSamplerResults
+    rng = np.random.default_rng(4)
+    M, P, N = 50, 3, 20
+    log_L = np.sort(rng.standard_normal(M)) * 3
+    log_dp = log_L + rng.standard_normal(M)
+    log_dp -= logsumexp(log_dp)
+    log_Z = -7.25
+    res = NestedSamplerResults(
+        log_Z_mean=log_Z, log_Z_uncert=0.1, ESS=10.0, H_mean=0.0, samples={}, parametrised_samples={},
+        U_samples=torch.tensor(rng.random((M, P))), log_L_samples=torch.tensor(log_L),
+        log_dp_mean=torch.tensor(log_dp), log_X_mean=None, log_posterior_density=None,
+        num_live_points_per_sample=None, num_likelihood_evaluations_per_sample=None, total_num_samples=M,
+        total_phantom_samples=0, total_num_likelihood_evaluations=0, log_efficiency=0.0, termination_reason=4)
+    ds = DeadSet.from_results(res, rng.standard_normal((N, P)), rng.standard_normal(N))
+    assert ds.U.dtype == torch.float64 and ds.log_w.dtype == torch.float64 and ds.Phi.dtype == torch.float32
+    np.testing.assert_allclose(ds.log_w.numpy(), log_dp - log_L + log_Z, rtol=1e-14)
+    assert logsumexp(log_L + ds.log_w.numpy()) == pytest.approx(log_Z, abs=1e-12)
