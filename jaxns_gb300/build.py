@@ -16,6 +16,10 @@ SOURCES = ["gbns_slice.cu", "gbns_slice_warp.cu", "gbns_ns.cu", "gbns_results.cu
            "gbns_static.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
+# Translation units whose fp32 arithmetic is reproduced bit for bit by a CPU model of the
+# kernels: no implicit multiply-add contraction, so every fused multiply-add is an explicit
+# fmaf in the source and the rounding sequence is the one written there.
+EXACT_FP32 = {"gbns_slice.cu", "gbns_slice_warp.cu", "gbns_ns.cu"}
 
 
 def _nvcc() -> str:
@@ -42,7 +46,8 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
 
     def compile_one(src):
         obj = os.path.join(OBJ_DIR, src.replace(".cu", ".o"))
-        cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-c", os.path.join(CSRC, src), "-o", obj]
+        extra = ["-fmad=false"] if src in EXACT_FP32 else []
+        cmd = [nvcc, *ARCH, *NVCC_FLAGS, *extra, "-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}:\n{r.stderr}")

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 #include "../../include/gbns.h"
+#include "gbns_fmath.h"
 
 #define GBNS_LN2 0.69314718055994530942
 #define GBNS_INV_LN2 1.44269504088896340736
@@ -58,17 +59,9 @@ __device__ __forceinline__ uint64_t bits64(Key k, uint32_t i) {
   return ((uint64_t)a << 32) | (uint64_t)b;
 }
 
-// Round-to-nearest-even conversion of a 64-bit unsigned integer to fp32 using 32-bit
-// operations only (a native 64-bit conversion runs on the FP64 pipe, which is scarce on
-// GB300): normalise, keep the top 32 bits with a sticky bit for the rest, convert, rescale.
-__device__ __forceinline__ float u64_to_float_rn(uint64_t x) {
-  if (x == 0ull) return 0.0f;
-  const int nz = __clzll(x);
-  const uint64_t y = x << nz;
-  const uint32_t top = (uint32_t)(y >> 32) | ((uint32_t)y != 0u ? 1u : 0u);
-  const float f = __uint2float_rn(top);                       // exact scale 2^(32 - nz) follows
-  return f * __int_as_float((127 + 32 - nz) << 23);           // 32 - nz in [-31, 32]
-}
+// Round-to-nearest-even conversion of a 64-bit unsigned integer to fp32 with 32-bit
+// operations only (gbns_fmath.h).
+__device__ __forceinline__ float u64_to_float_rn(uint64_t x) { return gbns_fm_u64_to_float(x); }
 
 // jax.random.uniform(float64) in [0,1) from 64 bits: the top 52 bits M give M * 2^-52;
 // rounded once to fp32.
@@ -76,20 +69,10 @@ __device__ __forceinline__ float uniform01(uint64_t b) {
   return u64_to_float_rn(b >> 12) * 2.220446049250313e-16f;  // 2^-52
 }
 
-// jax.random.normal(float64) = sqrt(2) * erfinv(u) with u = 2f - 1 + 2^-53, f = M * 2^-52
-// (M = top 52 bits), i.e. u = (4M + 1 - 2^53) * 2^-53 exactly.  Evaluated as
-// +-sqrt(2) * erfcinv(y) with y = 1 -+ u formed exactly from the integer M, so the tails keep
-// full relative precision in fp32.
-__device__ __forceinline__ float normal_from_bits(uint64_t b) {
-  const uint64_t M = b >> 12;
-  if (M >= (1ull << 51)) {
-    const uint64_t q = (1ull << 54) - 4ull * M - 1ull;  // (1 - u) * 2^53
-    return GBNS_SQRT2F * erfcinvf(u64_to_float_rn(q) * 1.1102230246251565e-16f);
-  } else {
-    const uint64_t q = 4ull * M + 1ull;  // (1 + u) * 2^53
-    return -GBNS_SQRT2F * erfcinvf(u64_to_float_rn(q) * 1.1102230246251565e-16f);
-  }
-}
+// jax.random.normal(float64) = sqrt(2) erfinv(u), u = (4M + 1 - 2^53) 2^-53 (M = top 52
+// bits): the standard normal quantile of p = (4M + 1) 2^-54 with |p - 1/2| and the tail mass
+// formed exactly from the integer M (gbns_fmath.h), so the tails keep full relative precision.
+__device__ __forceinline__ float normal_from_bits(uint64_t b) { return gbns_fm_normal_from_mantissa(b >> 12); }
 
 // ------------------------------------------------------------ log space ------
 
@@ -193,22 +176,37 @@ __device__ __forceinline__ int cta_and(int v, int *red) {
 // ----------------------------------------------------- FP64 evidence scan ----
 //
 // The recurrence of _update_evidence_calc_op (internals/shrinkage_statistics.py:43-94),
-// rewritten so that 32 elements are processed per warp step:
-//   X_k  = X_{k-1} T_k,            X2_k = X2_{k-1} T2_k                 (FP64 log-space sums)
+// rewritten as prefix sums so that a whole CTA processes blockDim elements per step:
+//   X_k  = X_{k-1} T_k,            X2_k = X2_{k-1} T2_k                 (FP64 log-space prefix sums)
 //   dZ_k = X_{k-1} t_k mid_k,      Z_k  = Z_{k-1} + dZ_k
-//   A_k  = ZX_k / X_k = A_{k-1} + X2_{k-1} tT_k mid_k / X_k              (plain sum)
+//   A_k  = ZX_k / X_k = A_{k-1} + X2_{k-1} tT_k mid_k / X_k              (an exclusive prefix sum)
 //   Z2_k = Z2_{k-1} + 2 X_{k-1} A_{k-1} t_k mid_k + X2_{k-1} t2_k mid_k^2
 //   dZ2_k = dZ2_{k-1} + X2_{k-1} t2_k mid_k^2
-// Sums are FP64 mantissas with an integer power-of-two exponent (rescaled exactly with
-// ldexp); each term is exp2 of an FP64 log-value offset by the chunk maximum, evaluated in
-// fp32 (the log-likelihoods are fp32).  Coefficients per n come from an FP64 table built
-// on the host with the reference formulas.
+// Every term is held as a scaled sum q 2^e: an exact power of two from the FP64 log-value and
+// an fp32-accurate mantissa, so no term loses relative precision however far it lies below
+// the others; sums are FP64 mantissas rescaled exactly by powers of two.  Z, Z2 and dZ2 are
+// accumulated per thread and reduced once at the end; log X, log X2 and A are CTA scans with
+// carries between chunks.  Coefficients per n come from an FP64 table built on the host with
+// the reference formulas.
 
 struct ScaledSum {
   double q;
   int e;  // value = q * 2^e  (q == 0 means zero)
 };
 
+// 2^k for k <= 1023 (0 below the normal range: the terms it scales are negligible there)
+__device__ __forceinline__ double pow2i(int k) {
+  return k < -1022 ? 0.0 : __longlong_as_double((long long)(k + 1023) << 52);
+}
+
+__device__ __forceinline__ ScaledSum ss_zero() {
+  ScaledSum s;
+  s.q = 0.0;
+  s.e = 0;
+  return s;
+}
+
+// exp(lv) with an FP64-exact exponent (register initialisation)
 __device__ __forceinline__ ScaledSum ss_from_log(double lv) {
   ScaledSum s;
   if (!(lv > -1e300)) { s.q = 0.0; s.e = 0; return s; }
@@ -219,20 +217,127 @@ __device__ __forceinline__ ScaledSum ss_from_log(double lv) {
   return s;
 }
 
+// exp(lv) as one term of a sum: exact power of two, mantissa in [1, 2) to fp32 precision
+__device__ __forceinline__ ScaledSum ss_term(double lv) {
+  ScaledSum s;
+  if (!(lv > -1e300)) { s.q = 0.0; s.e = 0; return s; }
+  const double y = lv * GBNS_INV_LN2;
+  const double f = floor(y);
+  s.q = (double)exp2f((float)(y - f));
+  s.e = (int)f;
+  return s;
+}
+
 __device__ __forceinline__ double ss_log(ScaledSum s) {
   if (!(s.q > 0.0)) return -INFINITY;
   return log(s.q) + (double)s.e * GBNS_LN2;
 }
 
-__device__ __forceinline__ void ss_add(ScaledSum &acc, double q, int e) {
-  if (!(q > 0.0)) return;
-  if (!(acc.q > 0.0)) { acc.q = q; acc.e = e; return; }
-  if (e > acc.e) {
-    acc.q = ldexp(acc.q, acc.e - e) + q;
-    acc.e = e;
+// a + b (commutative: the same bits either way round)
+__device__ __forceinline__ ScaledSum ss_sum(ScaledSum a, ScaledSum b) {
+  if (!(b.q > 0.0)) return a;
+  if (!(a.q > 0.0)) return b;
+  ScaledSum r;
+  if (a.e >= b.e) {
+    r.q = fma(b.q, pow2i(b.e - a.e), a.q);
+    r.e = a.e;
   } else {
-    acc.q += ldexp(q, e - acc.e);
+    r.q = fma(a.q, pow2i(a.e - b.e), b.q);
+    r.e = b.e;
   }
+  return r;
+}
+
+__device__ __forceinline__ ScaledSum shfl_up_ss(ScaledSum v, int o) {
+  ScaledSum r;
+  r.q = __shfl_up_sync(0xffffffffu, v.q, o);
+  r.e = __shfl_up_sync(0xffffffffu, v.e, o);
+  return r;
+}
+
+__device__ __forceinline__ ScaledSum shfl_xor_ss(ScaledSum v, int o) {
+  ScaledSum r;
+  r.q = __shfl_xor_sync(0xffffffffu, v.q, o);
+  r.e = __shfl_xor_sync(0xffffffffu, v.e, o);
+  return r;
+}
+
+struct EvScanSmem {
+  double wa[32], wb[32];
+  ScaledSum ws[32];
+  ScaledSum red[3][32];
+  double last_ldZ;
+  float last_L;
+};
+
+// Inclusive CTA scan of two FP64 sums; every thread also gets the CTA totals.
+__device__ __forceinline__ void cta_scan_d2(double &a, double &b, double &ta, double &tb, EvScanSmem &sm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double a2 = __shfl_up_sync(0xffffffffu, a, o), b2 = __shfl_up_sync(0xffffffffu, b, o);
+    if (lane >= o) {
+      a += a2;
+      b += b2;
+    }
+  }
+  if (lane == 31) {
+    sm.wa[w] = a;
+    sm.wb[w] = b;
+  }
+  __syncthreads();
+  if (w == 0) {
+    double x = lane < nw ? sm.wa[lane] : 0.0, y = lane < nw ? sm.wb[lane] : 0.0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const double x2 = __shfl_up_sync(0xffffffffu, x, o), y2 = __shfl_up_sync(0xffffffffu, y, o);
+      if (lane >= o) {
+        x += x2;
+        y += y2;
+      }
+    }
+    if (lane < nw) {
+      sm.wa[lane] = x;
+      sm.wb[lane] = y;
+    }
+  }
+  __syncthreads();
+  if (w > 0) {
+    a += sm.wa[w - 1];
+    b += sm.wb[w - 1];
+  }
+  ta = sm.wa[nw - 1];
+  tb = sm.wb[nw - 1];
+  __syncthreads();
+}
+
+// CTA scan of scaled sums: inclusive and exclusive prefix of each thread's value, and the total.
+__device__ __forceinline__ void cta_scan_ss(ScaledSum v, ScaledSum &incl, ScaledSum &excl, ScaledSum &tot,
+                                            EvScanSmem &sm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const ScaledSum u = shfl_up_ss(v, o);
+    if (lane >= o) v = ss_sum(u, v);
+  }
+  ScaledSum wex = shfl_up_ss(v, 1);
+  if (lane == 31) sm.ws[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    ScaledSum x = lane < nw ? sm.ws[lane] : ss_zero();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const ScaledSum u = shfl_up_ss(x, o);
+      if (lane >= o) x = ss_sum(u, x);
+    }
+    if (lane < nw) sm.ws[lane] = x;
+  }
+  __syncthreads();
+  const ScaledSum pw = w > 0 ? sm.ws[w - 1] : ss_zero();
+  incl = ss_sum(pw, v);
+  excl = lane == 0 ? pw : ss_sum(pw, wex);
+  tot = sm.ws[nw - 1];
+  __syncthreads();
 }
 
 struct EvAcc {
@@ -240,7 +345,6 @@ struct EvAcc {
   ScaledSum Z, A, Z2, dZ2;
   double ldZ_last;
   float Lprev;
-  bool lprev_valid;
 };
 
 __device__ __forceinline__ EvAcc evacc_from(const gbns_evcalc &e) {
@@ -288,63 +392,24 @@ __device__ __forceinline__ void ncoef_compute(double n, double *c) {
   c[4] = -lae(0.0, -lnn) - lnn2;
 }
 
-// Chunk-sum helper: every lane holds one FP64 log-term (or -inf); returns the warp sum as
-// (q, e) on all lanes.
-__device__ __forceinline__ void warp_logsum(double v, double &q, int &e) {
-  const float vf = (float)(v * GBNS_INV_LN2);
-  const float mx = warp_maxf(vf);
-  if (!(mx > -1e30f)) { q = 0.0; e = 0; return; }
-  e = (int)ceilf(mx) + 1;
-  const float t = (v > -1e300) ? exp2f((float)(v * GBNS_INV_LN2 - (double)e)) : 0.0f;
-  q = warp_sum((double)t);
-}
-
-// Inclusive warp scan of sum(exp(v)) as (q, e), value = q * 2^e: every lane keeps its own
-// power-of-two exponent so prefixes far below the chunk maximum keep their precision.
-__device__ __forceinline__ void warp_lse_incl_scan(double v, double &q, int &e) {
-  const int lane = threadIdx.x & 31;
-  if (v > -1e300) {
-    const double y = v * GBNS_INV_LN2;
-    e = (int)floor(y);
-    q = (double)exp2f((float)(y - (double)e));
-  } else {
-    q = 0.0;
-    e = 0;
-  }
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const double q2 = __shfl_up_sync(0xffffffffu, q, o);
-    const int e2 = __shfl_up_sync(0xffffffffu, e, o);
-    if (lane >= o && q2 > 0.0) {
-      if (!(q > 0.0)) {
-        q = q2;
-        e = e2;
-      } else if (e2 > e) {
-        q = ldexp(q, e - e2) + q2;
-        e = e2;
-      } else {
-        q += ldexp(q2, e2 - e);
-      }
-    }
-  }
-}
-
 // Process elements [0, M) of log-likelihoods L (fp32) with live-point counts given by
 // nmode: nconst > 0 -> n_k = nconst; ndesc > 0 -> n_k = ndesc - k; else n_k = narr[k].
-// Must be called by all 32 lanes of one warp.  Optional per-element outputs (FP64 logs).
-// L values are relative to Loff (added back in FP64); Lidx, when given, gathers L[Lidx[k]].
-__device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ L, long long M, int nconst, int ndesc,
-                                   const int *__restrict__ narr, const double *__restrict__ ncoef, int nmax,
-                                   double *__restrict__ out_lX, double *__restrict__ out_ldZ,
-                                   double *__restrict__ out_lZ, double Loff = 0.0,
-                                   const int *__restrict__ Lidx = nullptr) {
-  const int lane = threadIdx.x & 31;
-  for (long long base = 0; base < M; base += 32) {
-    const long long k = base + lane;
+// Called by every thread of the CTA (blockDim a multiple of 32).  Optional per-element
+// outputs (FP64 logs): log X, log dZ and, with OUT_LZ, the running log Z.  L values are
+// relative to Loff (added back in FP64); Lidx, when given, gathers L[Lidx[k]].
+template <bool OUT_LZ>
+__device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long long M, int nconst, int ndesc,
+                                  const int *__restrict__ narr, const double *__restrict__ ncoef, int nmax,
+                                  double *__restrict__ out_lX, double *__restrict__ out_ldZ,
+                                  double *__restrict__ out_lZ, double Loff, const int *__restrict__ Lidx,
+                                  EvScanSmem &sm) {
+  const int tid = threadIdx.x, T = blockDim.x;
+  ScaledSum pZ = ss_zero(), pZ2 = ss_zero(), pdZ2 = ss_zero();  // this thread's partial sums
+  for (long long base = 0; base < M; base += T) {
+    const long long k = base + tid;
     const bool valid = k < M;
     const float Lk = valid ? L[Lidx ? Lidx[k] : k] : 0.0f;
-    float Lm1 = __shfl_up_sync(0xffffffffu, Lk, 1);
-    if (lane == 0) Lm1 = acc.Lprev;
+    const float Lm1 = !valid ? 0.0f : (k == 0 ? acc.Lprev : L[Lidx ? Lidx[k - 1] : k - 1]);
     int nk = 1;
     if (valid) nk = nconst > 0 ? nconst : (ndesc > 0 ? (int)(ndesc - k) : narr[k]);
     nk = nk < 0 ? 0 : nk;
@@ -356,68 +421,73 @@ __device__ inline void evidence_scan_warp(EvAcc &acc, const float *__restrict__ 
       ncoef_compute((double)nk, cf);
     }
     const double lT = valid ? cf[0] : 0.0, lt = cf[1], lT2 = valid ? cf[2] : 0.0, lt2 = cf[3], ltT = cf[4];
-    // exclusive prefix of log T and log T2
-    const double sT = warp_incl_scan(lT), sT2 = warp_incl_scan(lT2);
+    double sT = lT, sT2 = lT2, totT, totT2;
+    cta_scan_d2(sT, sT2, totT, totT2, sm);
     const double lX_prev = acc.lX + (sT - lT), lX2_prev = acc.lX2 + (sT2 - lT2);
     const double lX_cur = acc.lX + sT;
     const double lmid = valid ? log_midpoint(Lk, Lm1) + Loff : -INFINITY;
     const double v_dZ = valid ? (lX_prev + lt) + lmid : -INFINITY;
     const double v_c = valid ? ((lX2_prev + ltT) + lmid) - lX_cur : -INFINITY;
     const double v_t2 = valid ? (lX2_prev + lt2) + 2.0 * lmid : -INFINITY;
-    // inclusive prefix of c in a chunk-local exponent
-    const float vcf = (float)(v_c * GBNS_INV_LN2);
-    const float mc = warp_maxf(vcf);
-    double cincl = 0.0, cterm = 0.0;
-    int ec = 0;
-    if (mc > -1e30f) {
-      ec = (int)ceilf(mc) + 1;
-      cterm = (v_c > -1e300) ? (double)exp2f((float)(v_c * GBNS_INV_LN2 - (double)ec)) : 0.0;
-      cincl = warp_incl_scan(cterm);
-    }
-    // log A_{k-1} = log(A0 + cexcl)
-    double lA_prev;
-    {
-      const double cex = cincl - cterm;
-      ScaledSum a = acc.A;
-      if (cex > 0.0) ss_add(a, cex, ec);
-      lA_prev = (a.q > 0.0) ? (double)logf((float)a.q) + (double)a.e * GBNS_LN2 : -INFINITY;
-    }
+    // A_{k-1} = A_0 + the exclusive prefix of c
+    ScaledSum cin, cex, ctot;
+    cta_scan_ss(ss_term(v_c), cin, cex, ctot, sm);
+    const ScaledSum Ap = ss_sum(acc.A, cex);
+    const double lA_prev = (Ap.q > 0.0) ? (double)logf((float)Ap.q) + (double)Ap.e * GBNS_LN2 : -INFINITY;
     const double v_t1 = valid ? ((GBNS_LN2 + lX_prev + lt) + lmid) + lA_prev : -INFINITY;
-    // per-element outputs
     if (valid) {
       if (out_lX) out_lX[k] = lX_cur;
       if (out_ldZ) out_ldZ[k] = v_dZ;
     }
-    // chunk sums
-    double q;
-    int e;
-    warp_logsum(v_dZ, q, e);
-    if (out_lZ) {
-      // running log Z per element (inclusive)
-      double incl;
-      int ee;
-      warp_lse_incl_scan(v_dZ, incl, ee);
-      ScaledSum z = acc.Z;
-      if (incl > 0.0) ss_add(z, incl, ee);
-      if (valid) out_lZ[k] = ss_log(z);
+    const ScaledSum tdZ = ss_term(v_dZ), tt2 = ss_term(v_t2);
+    if (OUT_LZ) {
+      ScaledSum zin, zex, ztot;
+      cta_scan_ss(tdZ, zin, zex, ztot, sm);
+      if (valid && out_lZ) out_lZ[k] = ss_log(ss_sum(acc.Z, zin));
+      acc.Z = ss_sum(acc.Z, ztot);
+    } else {
+      pZ = ss_sum(pZ, tdZ);
     }
-    ss_add(acc.Z, q, e);
-    double q1, q2;
-    int e1, e2;
-    warp_logsum(v_t1, q1, e1);
-    warp_logsum(v_t2, q2, e2);
-    ss_add(acc.Z2, q1, e1);
-    ss_add(acc.Z2, q2, e2);
-    ss_add(acc.dZ2, q2, e2);
-    // carry
-    const int last = (int)((M - base) < 32 ? (M - base - 1) : 31);
-    const double cin_last = __shfl_sync(0xffffffffu, cincl, 31);
-    if (cin_last > 0.0) ss_add(acc.A, cin_last, ec);
-    acc.lX = __shfl_sync(0xffffffffu, lX_cur, last);
-    acc.lX2 = acc.lX2 + __shfl_sync(0xffffffffu, sT2, last);
-    acc.ldZ_last = __shfl_sync(0xffffffffu, v_dZ, last);
-    acc.Lprev = __shfl_sync(0xffffffffu, Lk, last);
+    pZ2 = ss_sum(pZ2, ss_sum(ss_term(v_t1), tt2));
+    pdZ2 = ss_sum(pdZ2, tt2);
+    // carries into the next chunk (the same on every thread)
+    const long long last = (M - base < T ? M - base : T) - 1;
+    acc.lX += totT;
+    acc.lX2 += totT2;
+    acc.A = ss_sum(acc.A, ctot);
+    if (tid == last) {
+      sm.last_ldZ = v_dZ;
+      sm.last_L = Lk;
+    }
+    __syncthreads();
+    acc.ldZ_last = sm.last_ldZ;
+    acc.Lprev = sm.last_L;
+    __syncthreads();
   }
+  // CTA reduction of the partial sums (butterfly in each warp, then across warps)
+  const int lane = tid & 31, w = tid >> 5, nw = T >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    pZ = ss_sum(pZ, shfl_xor_ss(pZ, o));
+    pZ2 = ss_sum(pZ2, shfl_xor_ss(pZ2, o));
+    pdZ2 = ss_sum(pdZ2, shfl_xor_ss(pdZ2, o));
+  }
+  if (lane == 0) {
+    sm.red[0][w] = pZ;
+    sm.red[1][w] = pZ2;
+    sm.red[2][w] = pdZ2;
+  }
+  __syncthreads();
+  ScaledSum rZ = ss_zero(), rZ2 = ss_zero(), rdZ2 = ss_zero();
+  for (int q = 0; q < nw; ++q) {
+    rZ = ss_sum(rZ, sm.red[0][q]);
+    rZ2 = ss_sum(rZ2, sm.red[1][q]);
+    rdZ2 = ss_sum(rdZ2, sm.red[2][q]);
+  }
+  __syncthreads();
+  acc.Z = ss_sum(acc.Z, rZ);
+  acc.Z2 = ss_sum(acc.Z2, rZ2);
+  acc.dZ2 = ss_sum(acc.dZ2, rdZ2);
 }
 
 // ------------------------------------------------------------- likelihood ----
@@ -439,13 +509,9 @@ __device__ __forceinline__ void tf32_split(float x, float &hi, float &lo) {
 }
 
 // Standard-normal quantile of an FP64 u, evaluated in fp32 without losing the tails: the
-// argument handed to the fp32 inverse is formed exactly in FP64 (2u - 1 near the centre,
-// 2u or 2 - 2u in the tails), so u within 1e-12 of 0 or 1 still maps to its own quantile.
-__device__ __forceinline__ float ndtri_from_double(double u) {
-  const double z = 2.0 * u - 1.0;
-  if (fabs(z) < 0.5) return GBNS_SQRT2F * erfinvf((float)z);
-  return u < 0.5 ? -GBNS_SQRT2F * erfcinvf((float)(2.0 * u)) : GBNS_SQRT2F * erfcinvf((float)(2.0 - 2.0 * u));
-}
+// offset from 1/2 and the tail mass are formed in FP64 and rounded once (gbns_fmath.h), so u
+// within 1e-12 of 0 or 1 still maps to its own quantile.
+__device__ __forceinline__ float ndtri_from_double(double u) { return gbns_fm_ndtri_d(u); }
 
 // jax.random.uniform in FP64: the top 52 bits as the mantissa of [1, 2), minus 1.
 __device__ __forceinline__ double uniform01_d(uint64_t bits) {
@@ -459,7 +525,7 @@ __device__ __forceinline__ double uniform01_d(uint64_t bits) {
 // Prior quantiles: Uniform a + b u (b = high - low), Normal a + b ndtri(u) (b = scale).
 __device__ __forceinline__ float prior_quantile(int kind, float a, float b, float u) {
   if (kind == GBNS_PRIOR_UNIFORM) return fmaf(b, u, a);
-  return fmaf(b, GBNS_SQRT2F * erfinvf(fmaf(2.0f, u, -1.0f)), a);
+  return fmaf(b, gbns_fm_ndtri(u), a);
 }
 
 // Prior quantile x(u) and its slope dx/du (Uniform: b; Normal: b sqrt(2 pi) exp(z^2 / 2)),
@@ -469,9 +535,9 @@ __device__ __forceinline__ void prior_quantile_slope(int kind, float a, float b,
     x = fmaf(b, u, a);
     dxdu = b;
   } else {
-    const float z = GBNS_SQRT2F * erfinvf(fmaf(2.0f, u, -1.0f));
+    const float z = gbns_fm_ndtri(u);
     x = fmaf(b, z, a);
-    dxdu = b * 2.5066282746310002f * __expf(0.5f * z * z);
+    dxdu = b * 2.5066282746310002f * gbns_fm_exp(0.5f * z * z);
   }
 }
 

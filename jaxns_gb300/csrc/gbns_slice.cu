@@ -64,7 +64,7 @@ __device__ __forceinline__ void grad_u(const RunSmem<DMAX, FAM> &P, int D, const
     r2 = sqrtf(r2);
     const float z1 = (r1 - P.R) / P.w, z2 = (r2 - P.R) / P.w;
     const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2, mx = fmaxf(s1, s2);
-    const float q1 = __expf(s1 - mx), q2 = __expf(s2 - mx), tot = q1 + q2;
+    const float q1 = gbns_fm_exp(s1 - mx), q2 = gbns_fm_exp(s2 - mx), tot = q1 + q2;
     const float f1 = (q1 / tot) * (-z1 / P.w) / r1, f2 = (q2 / tot) * (-z2 / P.w) / r2;
 #pragma unroll
     for (int j = 0; j < DMAX; ++j)
@@ -111,7 +111,7 @@ __device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, cons
     const float z1 = (sqrtf(r1) - P.R) / P.w, z2 = (sqrtf(r2) - P.R) / P.w;
     const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
     const float m = fmaxf(s1, s2), dd = s1 - s2;
-    v = (dd != dd) ? s1 + s2 : m + log1pf(__expf(-fabsf(dd)));
+    v = (dd != dd) ? s1 + s2 : m + gbns_fm_log1p(gbns_fm_exp(-fabsf(dd)));
   }
   return (v != v) ? -INFINITY : v;  // NaN -> -inf (framework/ops.py:323-325)
 }
@@ -134,9 +134,11 @@ constexpr int slice_min_blocks() {
   return DMAX <= 8 ? 8 : ((DMAX == 16 && FAM == GBNS_LIK_SHELLS) ? 6 : (DMAX >= 64 ? 3 : 4));
 }
 
-// GRAD: the gradient-guided variant (the direction of slice j + 1 is the reflection of slice
-// j's direction about the U-space gradient at the accepted point); it keeps its gradient
-// arrays in registers at 2 CTAs per SM instead of spilling them.
+// GRAD: the gradient instantiation, for UniDimSliceSampler's two gradient options (runtime
+// flags of the batch): gradient_guided (the direction of slice j + 1 is the reflection of slice
+// j's direction about the U-space gradient at the accepted point) and gradient_slice (each
+// slice runs along the normalised gradient at its seed point, t in [0, right]); it keeps its
+// gradient arrays in registers at 2 CTAs per SM instead of spilling them.
 template <int DMAX, int FAM, bool GRAD>
 __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>()) k_slice_shell(gbns_batch b, int item_begin,
                                                                                  const float *__restrict__ Lstar_in,
@@ -169,7 +171,9 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
     }
   }
   const float Lstar = Lstar_in ? Lstar_in[r] : liveL[rd.s - 1];
+  __shared__ int s_next;
   if (threadIdx.x == 0) {
+    s_next = 0;
     if (FAM == GBNS_LIK_MVN) {
       P.c0 = fp[D + D * D];
     } else {
@@ -187,10 +191,11 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
   }
   __syncthreads();
 
-  // Every lane stays in the loop until its whole warp is done, so new directions can be
-  // generated warp-cooperatively; lanes past the item's chain count are idle from the start.
-  const bool valid = threadIdx.x < c_count;
-  const int c = c_begin + (valid ? threadIdx.x : 0);
+  // Chain pool: the CTA owns chains [c_begin, c_begin + c_count) of run r (at most a few per
+  // lane); a lane takes the next chain from the pool when its chain finishes, so the lanes of a
+  // warp stay busy until the pool is drained.  Every lane stays in the loop until its whole
+  // warp is done, so new directions can be generated warp-cooperatively.  A chain's arithmetic
+  // does not depend on the lane that runs it.
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   __shared__ float dirbuf[4][32][DMAX + 1];
   __shared__ uint4 dirkey[4][32];  // (direction key, lane) of each lane that needs a direction
@@ -205,43 +210,59 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
     const Key k0 = {st.key[0], st.key[1]};
     sample_key = fold(fold(k0, 0u), 1u);
   }
-  const Key kc = fold(sample_key, (uint32_t)c);
-  const Key chain_key = fold(kc, 0u), seed_key = fold(kc, 1u);
-
-  // --- seed point: resample_indicies over the mask log L > L* (internals/random.py:34-84)
   const int m = P.m;
-  int idx = 0;
-  if (m > 0) {
-    const uint64_t M52 = bits64(seed_key, 0u) >> 12;
-    const uint64_t q = (1ull << 52) - M52;  // (1 - U) * 2^52
-    const uint64_t lo = (uint64_t)m * q, hi = __umul64hi((uint64_t)m, q);
-    uint64_t kk = (hi << 12) | (lo >> 52);
-    if (lo & ((1ull << 52) - 1)) kk += 1;  // ceil(m (1 - U))
-    idx = (n - m) + (int)kk - 1;
-  }
+  const int budget = b.max_evals_per_slice;
+
+  int c = -1;          // current chain, -1 when the pool is drained
+  int j = S;           // slice index of the current chain (S: no chain)
+  bool start = true, need_dir = false, failed = false;
+  float left = 0.f, right = 0.f, t = 0.f, alpha = 0.5f, logL0 = 0.f;
+  Key ck = {0u, 0u}, after_key = {0u, 0u}, slices_key = {0u, 0u}, dir_key = {0u, 0u};
+  int total = 0, in_slice = 0;
   float u0[DMAX], d[DMAX];
 #pragma unroll
-  for (int j = 0; j < DMAX; ++j) {
-    u0[j] = (valid && j < D) ? liveU[(size_t)idx * D + j] : 0.0f;
-    d[j] = 0.0f;
+  for (int q = 0; q < DMAX; ++q) {
+    u0[q] = 0.0f;
+    d[q] = 0.0f;
   }
-  float logL0 = liveL[idx];
 
-  const Key slices_key = fold(chain_key, 1u);
-  Key dir_key = fold(chain_key, 0u);  // _sample_direction(direction_key) of get_sample_from_seed
-  bool need_dir = valid;
+  // next chain of the pool: keys, seed point (resample_indicies over the mask log L > L*,
+  // internals/random.py:34-84), first direction key (get_sample_from_seed)
+  auto grab = [&]() {
+    const int q = atomicAdd(&s_next, 1);
+    if (q >= c_count) {
+      c = -1;
+      j = S;
+      return;
+    }
+    c = c_begin + q;
+    const Key kc = fold(sample_key, (uint32_t)c);
+    const Key chain_key = fold(kc, 0u), seed_key = fold(kc, 1u);
+    int idx = 0;
+    if (m > 0) {
+      const uint64_t M52 = bits64(seed_key, 0u) >> 12;
+      const uint64_t qq = (1ull << 52) - M52;  // (1 - U) * 2^52
+      const uint64_t lo = (uint64_t)m * qq, hi = __umul64hi((uint64_t)m, qq);
+      uint64_t kk = (hi << 12) | (lo >> 52);
+      if (lo & ((1ull << 52) - 1)) kk += 1;  // ceil(m (1 - U))
+      idx = (n - m) + (int)kk - 1;
+    }
+#pragma unroll
+    for (int q2 = 0; q2 < DMAX; ++q2)
+      if (q2 < D) u0[q2] = liveU[(size_t)idx * D + q2];
+    logL0 = liveL[idx];
+    slices_key = fold(chain_key, 1u);
+    dir_key = fold(chain_key, 0u);
+    need_dir = true;
+    j = 0;
+    start = true;
+    total = 0;
+    in_slice = 0;
+    failed = false;
+  };
+  grab();
 
   // --- flattened slice / shrink loop
-  int j = valid ? 0 : S;
-  bool start = true;
-  float left = 0.f, right = 0.f, t = 0.f, alpha = 0.5f;
-  Key ck = {0u, 0u}, after_key = {0u, 0u};
-  int total = 0, in_slice = 0;
-  const int budget = b.max_evals_per_slice;
-  const size_t out = (size_t)rd.shell_off + c;
-  float *phU = b.ph_U + rd.phU_off + (size_t)c * K * D;
-  float *phL = b.ph_L + rd.phL_off + (size_t)c * K;
-  bool failed = false;
   for (;;) {
     // ---- new directions: the D normals of every lane that needs one, flattened over
     // (lane, dimension) pairs across the warp; lanes publish their keys in rank order
@@ -269,10 +290,10 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
               d[q] = dirbuf[wid][lane][q];
               ss = fmaf(d[q], d[q], ss);
             }
-          const float nrm = sqrtf(ss);
+          const float inv = 1.0f / sqrtf(ss);
 #pragma unroll
           for (int q = 0; q < DMAX; ++q)
-            if (q < D) d[q] = d[q] / nrm;
+            if (q < D) d[q] = d[q] * inv;
         }
         __syncwarp();
       }
@@ -291,13 +312,33 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
     if (start) {
       after_key = fold(B, 3u);
       alpha = slice_alpha(j, S);
-      // _slice_bounds (uni_slice_sampler.py:41-64)
+      bool climb = false;
+      if (GRAD && b.gradient_slice) {
+        // gradient_slice (uni_slice_sampler.py:202-214): slice along the normalised U-space
+        // gradient at the seed point unless it vanishes or is not finite; one evaluation
+        float g[DMAX];
+        grad_u<DMAX, FAM>(P, D, u0, g);
+        ++total;
+        float gg = 0.0f;
+#pragma unroll
+        for (int q = 0; q < DMAX; ++q)
+          if (q < D) gg = fmaf(g[q], g[q], gg);
+        const float gn = sqrtf(gg);
+        if (gn != 0.0f && isfinite(gn)) {
+          climb = true;
+#pragma unroll
+          for (int q = 0; q < DMAX; ++q)
+            if (q < D) d[q] = g[q] / gn;
+        }
+      }
+      // _slice_bounds (uni_slice_sampler.py:41-64), with one reciprocal per direction component
       float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
 #pragma unroll
       for (int q = 0; q < DMAX; ++q) {
         if (q < D) {
-          const float t1 = (1.0f - u0[q]) / d[q];
-          const float t0 = -u0[q] / d[q];
+          const float rc = 1.0f / d[q];
+          const float t1 = (1.0f - u0[q]) * rc;
+          const float t0 = -u0[q] * rc;
           t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
           t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
           t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
@@ -305,7 +346,7 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
         }
       }
       right = fminf(t0r, t1r);
-      left = fmaxf(t0l, t1l);
+      left = climb ? 0.0f : fmaxf(t0l, t1l);  // climbing: only t >= 0 (uni_slice_sampler.py:214)
       in_slice = 0;
     } else {
       // _shrink_interval (uni_slice_sampler.py:92-111)
@@ -331,12 +372,13 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
       logL0 = logL;
       const int p = j - (S - 1 - K);
       if (K > 0 && p >= 0 && j < S - 1) {
-        for (int q = 0; q < D; ++q) phU[(size_t)p * D + q] = u0[q];
-        phL[p] = logL;
+        float *phU = b.ph_U + rd.phU_off + ((size_t)c * K + p) * D;
+        for (int q = 0; q < D; ++q) phU[q] = u0[q];
+        b.ph_L[rd.phL_off + (size_t)c * K + p] = logL;
       }
       ++j;
       start = true;
-      if (GRAD) {
+      if (GRAD && b.gradient_guided) {
         // Householder reflection at the accepted point (uni_slice_sampler.py:255-269); a
         // random direction from split(after_key)[0] when the gradient vanishes or is not
         // finite.  The gradient counts as one likelihood evaluation, also after the last slice.
@@ -374,16 +416,20 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
         need_dir = true;
         dir_key = after_key;
       }
+      if (j >= S) {
+        // chain finished: outputs, then the next chain of the pool
+        const size_t out = (size_t)rd.shell_off + c;
+        float *nu = b.new_U + rd.newU_off + (size_t)c * D;
+        for (int q = 0; q < D; ++q) nu[q] = u0[q];
+        b.new_L[out] = logL0;
+        b.new_E[out] = total;
+        if (failed) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
+        grab();
+      }
     } else {
       start = false;
     }
   }
-  if (!valid) return;
-  float *nu = b.new_U + rd.newU_off + (size_t)c * D;
-  for (int q = 0; q < D; ++q) nu[q] = u0[q];
-  b.new_L[out] = logL0;
-  b.new_E[out] = total;
-  if (failed) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
 }
 
 template <int DMAX>
@@ -395,11 +441,13 @@ static cudaError_t launch_bucket(const gbns_batch &b, int fam, int ib, int ie, c
   constexpr int DM = DMAX <= 16 ? DMAX : 16;
   if (fam == GBNS_LIK_MVN) {
     if (DMAX <= 16) {
-      if (b.gradient_guided) k_slice_shell<DM, GBNS_LIK_MVN, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+      if (b.gradient_guided || b.gradient_slice)
+        k_slice_shell<DM, GBNS_LIK_MVN, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
       else k_slice_shell<DM, GBNS_LIK_MVN, false><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
     }
   } else {
-    if (b.gradient_guided) k_slice_shell<DMAX, GBNS_LIK_SHELLS, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+    if (b.gradient_guided || b.gradient_slice)
+      k_slice_shell<DMAX, GBNS_LIK_SHELLS, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
     else k_slice_shell<DMAX, GBNS_LIK_SHELLS, false><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
   }
   return cudaGetLastError();

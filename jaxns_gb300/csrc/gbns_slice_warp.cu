@@ -155,6 +155,46 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
   };
   grab();
 
+  // U-space gradient of log L at column q of U0, lanes over dimensions (j0, j1): e = x - mu,
+  // z = Linv e, g = -Linv^T z, times the prior quantile's slope; columns 0 and 1 of the
+  // proposal scratch hold e and z (the proposals of this step are written after it)
+  auto grad_col = [&](int q, float &g0, float &g1) {
+    float e0 = 0.f, e1 = 0.f, s0 = 0.f, s1 = 0.f;
+    if (j0 < D) {
+      float x;
+      prior_quantile_slope(pkind[j0], pa[j0], pb[j0], V.U0[j0][q], x, s0);
+      e0 = x - pmu[j0];
+    }
+    if (DMAX > 32 && j1 < D) {
+      float x;
+      prior_quantile_slope(pkind[j1], pa[j1], pb[j1], V.U0[j1][q], x, s1);
+      e1 = x - pmu[j1];
+    }
+    __syncwarp();
+    V.DEL[j0][0] = e0;
+    if (DMAX > 32) V.DEL[j1][0] = e1;
+    __syncwarp();
+    float z0 = 0.f, z1 = 0.f;
+    for (int k = 0; k < D; ++k) {
+      const float ek = V.DEL[k][0];
+      z0 = fmaf(LinvT[k * DMAX + j0], ek, z0);
+      if (DMAX > 32) z1 = fmaf(LinvT[k * DMAX + j1], ek, z1);
+    }
+    V.DEL[j0][1] = z0;
+    if (DMAX > 32) V.DEL[j1][1] = z1;
+    __syncwarp();
+    g0 = 0.f;
+    g1 = 0.f;
+    for (int i = 0; i < D; ++i) {
+      const float zi = V.DEL[i][1];
+      g0 = fmaf(LinvT[j0 * DMAX + i], zi, g0);
+      if (DMAX > 32) g1 = fmaf(LinvT[j1 * DMAX + i], zi, g1);
+    }
+    g0 = -g0 * s0;
+    g1 = -g1 * s1;
+    __syncwarp();
+  };
+
   for (;;) {
     // ---- new directions (initial or after an accepted slice), lane-parallel over dims
     unsigned dm = __ballot_sync(0xffffffffu, need_dir);
@@ -183,6 +223,20 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
     while (sm_) {
       const int q = __ffs(sm_) - 1;
       sm_ &= sm_ - 1;
+      bool climb = false;
+      if (GRAD && b.gradient_slice) {
+        // gradient_slice (uni_slice_sampler.py:202-214): slice along the normalised gradient at
+        // the seed point unless it vanishes or is not finite (one evaluation, counted below)
+        float g0, g1;
+        grad_col(q, g0, g1);
+        const float gn = sqrtf(warp_sum(fmaf(g0, g0, g1 * g1)));
+        if (gn != 0.0f && isfinite(gn)) {
+          climb = true;
+          if (j0 < D) V.DIR[j0][q] = g0 / gn;
+          if (DMAX > 32 && j1 < D) V.DIR[j1][q] = g1 / gn;
+        }
+        __syncwarp();
+      }
       float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
 #pragma unroll
       for (int h = 0; h < (DMAX > 32 ? 2 : 1); ++h) {
@@ -204,7 +258,8 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
       }
       if (lane == q) {
         right = rgt;
-        left = lft;
+        left = climb ? 0.0f : lft;  // climbing: only t >= 0 (uni_slice_sampler.py:214)
+        if (GRAD && b.gradient_slice) ++total;
       }
     }
 
@@ -308,43 +363,14 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
     }
     __syncwarp();
     bool grad_fallback = false;
-    if (GRAD) {
+    if (GRAD && b.gradient_guided) {
       // reflect each advancing chain's direction about the gradient at its accepted point
       unsigned mm = am;
       while (mm) {
         const int q = __ffs(mm) - 1;
         mm &= mm - 1;
-        float e0 = 0.f, e1 = 0.f, s0 = 0.f, s1 = 0.f;
-        if (j0 < D) {
-          float x;
-          prior_quantile_slope(pkind[j0], pa[j0], pb[j0], V.U0[j0][q], x, s0);
-          e0 = x - pmu[j0];
-        }
-        if (DMAX > 32 && j1 < D) {
-          float x;
-          prior_quantile_slope(pkind[j1], pa[j1], pb[j1], V.U0[j1][q], x, s1);
-          e1 = x - pmu[j1];
-        }
-        V.DEL[j0][0] = e0;
-        if (DMAX > 32) V.DEL[j1][0] = e1;
-        __syncwarp();
-        float z0 = 0.f, z1 = 0.f;  // z = Linv e, rows j0, j1
-        for (int k = 0; k < D; ++k) {
-          const float ek = V.DEL[k][0];
-          z0 = fmaf(LinvT[k * DMAX + j0], ek, z0);
-          if (DMAX > 32) z1 = fmaf(LinvT[k * DMAX + j1], ek, z1);
-        }
-        V.DEL[j0][1] = z0;
-        if (DMAX > 32) V.DEL[j1][1] = z1;
-        __syncwarp();
-        float g0 = 0.f, g1 = 0.f;  // -Linv^T z, rows j0, j1
-        for (int i = 0; i < D; ++i) {
-          const float zi = V.DEL[i][1];
-          g0 = fmaf(LinvT[j0 * DMAX + i], zi, g0);
-          if (DMAX > 32) g1 = fmaf(LinvT[j1 * DMAX + i], zi, g1);
-        }
-        g0 = -g0 * s0;
-        g1 = -g1 * s1;
+        float g0, g1;
+        grad_col(q, g0, g1);
         const float gn = sqrtf(warp_sum(fmaf(g0, g0, g1 * g1)));
         if (!(gn >= 1e-10f) || isinf(gn)) {
           if (lane == q) grad_fallback = true;
@@ -369,9 +395,9 @@ __global__ void __launch_bounds__(32 * (DMAX == 64 ? WARPS_PER_CTA_64 : WARPS_PE
       }
       ++j;
       start = true;
-      if (GRAD) ++total;  // the gradient counts as one likelihood evaluation
+      if (GRAD && b.gradient_guided) ++total;  // the gradient counts as one likelihood evaluation
       if (j < S) {
-        if (!GRAD) {
+        if (!(GRAD && b.gradient_guided)) {
           need_dir = true;
           dir_key = after_key;
         } else if (grad_fallback) {
@@ -416,7 +442,8 @@ static cudaError_t launch_warp_bucket(const gbns_batch &b, int ib, int ie, const
     if (e != cudaSuccess) return e;
     configured = true;
   }
-  if (b.gradient_guided) k_slice_mvn_warp<DMAX, true><<<nblk, 32 * warps, sm, stream>>>(b, ib, Lstar, keys);
+  if (b.gradient_guided || b.gradient_slice)
+    k_slice_mvn_warp<DMAX, true><<<nblk, 32 * warps, sm, stream>>>(b, ib, Lstar, keys);
   else k_slice_mvn_warp<DMAX, false><<<nblk, 32 * warps, sm, stream>>>(b, ib, Lstar, keys);
   return cudaGetLastError();
 }

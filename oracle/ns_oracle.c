@@ -133,6 +133,9 @@ typedef struct {
     const double *prior_b;   /* [D] uniform: high - low; normal: scale */
     const double *p;         /* family parameters */
     int N;                   /* rows of Phi for the linear-Gaussian family */
+    const double *prior_A;   /* [D x D] lower triangular, or NULL: X = A q + c after the per-dimension
+                                quantiles q (MultivariateNormalTriL blocks: the bijector loc + L z) */
+    const double *prior_c;   /* [D] */
 } orc_model;
 
 /* U -> X: the prior quantile (tfp Uniform / Normal quantile as used by
@@ -143,6 +146,17 @@ static void prior_transform(const orc_model *m, const double *U, double *X) {
             X[j] = m->prior_a[j] + m->prior_b[j] * U[j];
         else
             X[j] = m->prior_a[j] + m->prior_b[j] * (ORC_SQRT2 * orc_erfinv(2.0 * U[j] - 1.0));
+    }
+    if (m->prior_A) {
+        /* tfp MultivariateNormalTriL: the bijector loc + L z after the base quantile
+         * (framework/wrapped_tfp_distribution.py:77-84); rows from the last, so X[k], k <= i,
+         * still hold the quantiles */
+        int D = m->D;
+        for (int i = D - 1; i >= 0; --i) {
+            double acc = m->prior_c[i];
+            for (int k = 0; k <= i; ++k) acc += m->prior_A[i * D + k] * X[k];
+            X[i] = acc;
+        }
     }
 }
 
@@ -254,6 +268,16 @@ void orc_grad_U(const orc_model *m, const double *U, double *g) {
             for (int j = 0; j < D; ++j) gx[j] += Phi[(size_t)i * D + j] * r / (sigma * sigma);
         }
     }
+    if (m->prior_A) {
+        /* d log L / dq = A^T d log L / dX */
+        double gq[128];
+        for (int k = 0; k < D; ++k) {
+            double acc = 0.0;
+            for (int i = k; i < D; ++i) acc += m->prior_A[i * D + k] * gx[i];
+            gq[k] = acc;
+        }
+        for (int k = 0; k < D; ++k) gx[k] = gq[k];
+    }
     for (int j = 0; j < D; ++j) {
         double dxdu;
         if (m->prior_kind[j] == ORC_PRIOR_UNIFORM) {
@@ -313,6 +337,7 @@ typedef struct {
     int num_phantom;
     int midpoint_shrink;
     int gradient_guided;
+    int gradient_slice;
 } orc_slice_cfg;
 
 /* linspace(0.5, 1., S)[j] as jnp.linspace evaluates it. */
@@ -327,16 +352,32 @@ static double slice_alpha(int j, int S) {
  * U0/logL0 is the seed; on return U holds the accepted point, d the new direction. */
 static double new_proposal(const orc_model *m, okey key, const double *U0, double logL0,
                            double *d, int midpoint, double alpha, double Lstar, double *U,
-                           long *nevals, int gradient_guided) {
+                           long *nevals, int gradient_guided, int gradient_slice) {
     int D = m->D;
     okey run_key = key_fold(key, 0);
     okey t_key = key_fold(key, 2);
     okey after_key = key_fold(key, 3);
     double left, right;
+    long ne = 0;
+    int climb = 0;
+    if (gradient_slice) {
+        /* climb the gradient (uni_slice_sampler.py:202-214): slice along the normalised U-space
+         * gradient at the seed point, t >= 0, unless the gradient vanishes or is not finite */
+        double g[128], gn = 0.0;
+        orc_grad_U(m, U0, g);
+        ne += 1;
+        for (int j = 0; j < D; ++j) gn += g[j] * g[j];
+        gn = sqrt(gn);
+        if (!(gn == 0.0 || !isfinite(gn))) {
+            for (int j = 0; j < D; ++j) d[j] = g[j] / gn;
+            climb = 1;
+        }
+    }
     slice_bounds(U0, d, D, &left, &right);
+    if (climb) left = 0.0;
     double t = pick_point(t_key, U0, d, D, left, right, U);
     double logL = orc_forward(m, U);
-    long ne = 1;
+    ne += 1;
     okey ck = run_key;
     while (!((logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar)))) {
         okey nk = key_fold(ck, 0);
@@ -426,7 +467,7 @@ void orc_slice_get_sample(const orc_model *m, const orc_slice_cfg *cfg, uint32_t
         okey kj = key_fold(slices_key, (uint64_t)j);
         long ne;
         double logL = new_proposal(m, kj, U0, logL0, d, cfg->midpoint_shrink, slice_alpha(j, S), Lstar,
-                                   U, &ne, cfg->gradient_guided);
+                                   U, &ne, cfg->gradient_guided, cfg->gradient_slice);
         total += ne;
         memcpy(U0, U, sizeof(double) * D);
         logL0 = logL;
@@ -610,7 +651,11 @@ void orc_count_crossed_edges(const long *sender, const double *log_L, long N, lo
     nodes[0] = -INFINITY;
     for (long i = 0; i < N; ++i) nodes[i + 1] = log_L[i];
     orc_stable_argsort(nodes, N + 1, perm);
-    for (long i = 0; i < N; ++i) deg[sender[i] > 0 ? sender[i] : 0] += 1;
+    /* out_degree.at[max(sender, 0)].add(1): scatter updates outside [0, N] are dropped (jax) */
+    for (long i = 0; i < N; ++i) {
+        long sd = sender[i] > 0 ? sender[i] : 0;
+        if (sd <= N) deg[sd] += 1;
+    }
     long fake = num_samples >= 0 ? (N - num_samples) : 0;
     long stop = num_samples >= 0 ? num_samples : N + 1;
     long crossed = 1;
@@ -1161,3 +1206,342 @@ void orc_ns_run_batch(const orc_model *models, const orc_ns_cfg *cfgs, const orc
     free(th);
     pthread_mutex_destroy(&j.mu);
 }
+
+/* =====================================================================================
+ * fp32 kernel-arithmetic mode.
+ *
+ * The device chains compute in fp32 (U, directions, interval, log-likelihoods relative to
+ * the run's FP64 offset) and use the elementary functions of gbns_fmath.h, which are built
+ * from correctly rounded IEEE operations only.  This section restates the same chain
+ * algorithm (uni_slice_sampler.py:114-273, :343-441; bases.py:63-75; random.py:34-84) in
+ * exactly the kernels' fp32 operation order, so that each chain's evaluation count,
+ * accepted point and log-likelihood can be compared bit for bit.  It differs from the FP64
+ * restatement above only in precision and in the order of the two fp32 reductions the
+ * kernels perform (sequential per thread, or a butterfly across the 32 lanes of a warp
+ * in the warp-cooperative correlated-Gaussian kernel); the RNG stream, the seed choice, the
+ * accept test and the shrink rule are the same.
+ * ===================================================================================== */
+
+#include "../jaxns_gb300/csrc/gbns_fmath.h"
+
+typedef struct {
+    int D;
+    int family;               /* ORC_LIK_MVN or ORC_LIK_SHELLS */
+    const int *prior_kind;    /* [D] */
+    const float *prior_a;     /* [D] fp32, as the device holds it */
+    const float *prior_b;     /* [D] */
+    const float *p;           /* fp32 parameters in the device layout: MVN [mu, Linv (row-major lower), c0];
+                                 shells [c1, c2, R, w, norm] */
+    int variant;              /* 0: one thread per chain; 32 / 64: warp-cooperative MVN kernel of that DMAX */
+} orc32_model;
+
+static inline float o32_uniform(okey k) { return gbns_fm_u64_to_float(bits64(k, 0) >> 12) * 0x1p-52f; }
+
+static inline float o32_quantile(const orc32_model *m, int j, float u) {
+    if (m->prior_kind[j] == ORC_PRIOR_UNIFORM) return fmaf(m->prior_b[j], u, m->prior_a[j]);
+    return fmaf(m->prior_b[j], gbns_fm_ndtri(u), m->prior_a[j]);
+}
+
+/* Sum of the squared rows z_i (i < D) of the warp kernel's register tile: rows 8g..8g+7
+ * (and 32+8g.. for DMAX 64) summed per lane group g in order, then (S0 + S1) + (S2 + S3). */
+static float o32_warp_sumsq(const float *z, int D, int dmax) {
+    float S[4];
+    for (int g = 0; g < 4; ++g) {
+        float s = 0.0f;
+        for (int p = 0; p < dmax / 32; ++p) {
+            if (32 * p >= D) continue;
+            for (int rr = 0; rr < 8; ++rr) {
+                int row = 32 * p + 8 * g + rr;
+                float a = row < D ? z[row] : 0.0f;
+                s = fmaf(a, a, s);
+            }
+        }
+        S[g] = s;
+    }
+    return (S[0] + S[1]) + (S[2] + S[3]);
+}
+
+/* 32-lane butterfly sum (__shfl_xor over 16, 8, 4, 2, 1); every lane ends with this value */
+static float o32_butterfly(const float *a_in) {
+    float a[32], b[32];
+    memcpy(a, a_in, sizeof a);
+    for (int o = 16; o > 0; o >>= 1) {
+        for (int l = 0; l < 32; ++l) b[l] = a[l] + a[l ^ o];
+        memcpy(a, b, sizeof a);
+    }
+    return a[0];
+}
+
+/* log L(u) - offset, fp32, of the point u = u0 + t d (Model.forward, framework/model.py:167;
+ * NaN -> -inf, framework/ops.py:323-325) */
+static float o32_loglik_line(const orc32_model *m, const float *u0, const float *d, float t) {
+    int D = m->D;
+    float x[128];
+    for (int j = 0; j < D; ++j) x[j] = o32_quantile(m, j, fmaf(t, d[j], u0[j]));
+    float v;
+    if (m->family == ORC_LIK_MVN) {
+        const float *mu = m->p, *Linv = m->p + D;
+        float z[128];
+        for (int j = 0; j < D; ++j) x[j] = x[j] - mu[j];
+        for (int i = 0; i < D; ++i) {
+            float acc = 0.0f;
+            for (int j = 0; j <= i; ++j) acc = fmaf(Linv[i * D + j], x[j], acc);
+            z[i] = acc;
+        }
+        float s;
+        if (m->variant == 0) {
+            s = 0.0f;
+            for (int i = 0; i < D; ++i) s = fmaf(z[i], z[i], s);
+        } else {
+            s = o32_warp_sumsq(z, D, m->variant);
+        }
+        v = -0.5f * s;
+    } else {
+        const float *c1 = m->p, *c2 = m->p + D;
+        float R = m->p[2 * D], w = m->p[2 * D + 1];
+        float r1 = 0.0f, r2 = 0.0f;
+        for (int j = 0; j < D; ++j) {
+            float e1 = x[j] - c1[j], e2 = x[j] - c2[j];
+            r1 = fmaf(e1, e1, r1);
+            r2 = fmaf(e2, e2, r2);
+        }
+        float z1 = (sqrtf(r1) - R) / w, z2 = (sqrtf(r2) - R) / w;
+        float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
+        float mx = fmaxf(s1, s2), dd = s1 - s2;
+        v = (dd != dd) ? s1 + s2 : mx + gbns_fm_log1p(gbns_fm_exp(-fabsf(dd)));
+    }
+    return (v != v) ? -INFINITY : v;
+}
+
+float orc32_forward(const orc32_model *m, const float *U) {
+    float zero[128];
+    memset(zero, 0, sizeof zero);
+    return o32_loglik_line(m, U, zero, 0.0f);
+}
+
+void orc32_forward_batch(const orc32_model *m, const float *U, long B, float *out) {
+    for (long b = 0; b < B; ++b) out[b] = orc32_forward(m, U + b * m->D);
+}
+
+/* U-space gradient of log L - offset in the thread kernel's fp32 arithmetic (jax.grad of
+ * Model.forward through the prior quantile: Uniform dx/du = b, Normal dx/du = b sqrt(2 pi)
+ * exp(z^2 / 2)); correlated Gaussian -Linv^T Linv (x - mu), shells the softmax-weighted radial
+ * terms. */
+static void o32_grad_u(const orc32_model *m, const float *u, float *g) {
+    int D = m->D;
+    float x[128], dxdu[128];
+    for (int j = 0; j < D; ++j) {
+        if (m->prior_kind[j] == ORC_PRIOR_UNIFORM) {
+            x[j] = fmaf(m->prior_b[j], u[j], m->prior_a[j]);
+            dxdu[j] = m->prior_b[j];
+        } else {
+            float z = gbns_fm_ndtri(u[j]);
+            x[j] = fmaf(m->prior_b[j], z, m->prior_a[j]);
+            dxdu[j] = m->prior_b[j] * 2.5066282746310002f * gbns_fm_exp(0.5f * z * z);
+        }
+    }
+    if (m->family == ORC_LIK_MVN) {
+        const float *mu = m->p, *Linv = m->p + D;
+        float e[128], zz[128];
+        for (int j = 0; j < D; ++j) e[j] = x[j] - mu[j];
+        for (int i = 0; i < D; ++i) {
+            float acc = 0.0f;
+            for (int j = 0; j <= i; ++j) acc = fmaf(Linv[i * D + j], e[j], acc);
+            zz[i] = acc;
+        }
+        for (int q = 0; q < D; ++q) {
+            float acc = 0.0f;
+            for (int i = q; i < D; ++i) acc = fmaf(Linv[i * D + q], zz[i], acc);
+            g[q] = -acc * dxdu[q];
+        }
+    } else {
+        const float *c1 = m->p, *c2 = m->p + D;
+        float R = m->p[2 * D], w = m->p[2 * D + 1];
+        float r1 = 0.f, r2 = 0.f;
+        for (int j = 0; j < D; ++j) {
+            float e1 = x[j] - c1[j], e2 = x[j] - c2[j];
+            r1 = fmaf(e1, e1, r1);
+            r2 = fmaf(e2, e2, r2);
+        }
+        r1 = sqrtf(r1);
+        r2 = sqrtf(r2);
+        float z1 = (r1 - R) / w, z2 = (r2 - R) / w;
+        float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2, mx = fmaxf(s1, s2);
+        float q1 = gbns_fm_exp(s1 - mx), q2 = gbns_fm_exp(s2 - mx), tot = q1 + q2;
+        float f1 = (q1 / tot) * (-z1 / w) / r1, f2 = (q2 / tot) * (-z2 / w) / r2;
+        for (int j = 0; j < D; ++j) g[j] = (f1 * (x[j] - c1[j]) + f2 * (x[j] - c2[j])) * dxdu[j];
+    }
+}
+
+/* _sample_direction (uni_slice_sampler.py:23-38): D normals, normalised by one reciprocal of
+ * the norm (sum of squares sequential per thread, or the warp kernel's butterfly). */
+static void o32_direction(const orc32_model *m, okey k, float *d) {
+    int D = m->D;
+    if (D == 1) { d[0] = 1.0f; return; }
+    float v[128];
+    for (int j = 0; j < D; ++j) v[j] = gbns_fm_normal_from_mantissa(bits64(k, (uint64_t)j) >> 12);
+    float ss;
+    if (m->variant == 0) {
+        ss = 0.0f;
+        for (int j = 0; j < D; ++j) ss = fmaf(v[j], v[j], ss);
+    } else {
+        float a[32];
+        for (int l = 0; l < 32; ++l) {
+            float v0 = l < D ? v[l] : 0.0f;
+            float v1 = (m->variant > 32 && l + 32 < D) ? v[l + 32] : 0.0f;
+            a[l] = fmaf(v1, v1, v0 * v0);
+        }
+        ss = o32_butterfly(a);
+    }
+    float inv = 1.0f / sqrtf(ss);
+    for (int j = 0; j < D; ++j) d[j] = v[j] * inv;
+}
+
+/* linspace(0.5, 1, S)[j] in fp32 */
+static float o32_alpha(int j, int S) {
+    if (S == 1) return 0.5f;
+    if (j == S - 1) return 1.0f;
+    float step = (float)j / (float)(S - 1);
+    return 0.5f * (1.0f - step) + step;
+}
+
+/* One chain (UniDimSliceSampler.get_sample) in the kernels' fp32 arithmetic: chain key kc =
+ * split(sample_key, s)[c]; returns the accepted point, its log L (relative) and the number
+ * of evaluations.  Phantoms: [K, D] and [K]. */
+void orc32_slice_chain(const orc32_model *m, const orc_slice_cfg *cfg, uint32_t k0, uint32_t k1, float Lstar,
+                       const float *live_U, const float *live_L, long n, long max_evals_per_slice, float *U_out,
+                       float *L_out, long *E_out, float *ph_U, float *ph_L) {
+    int D = m->D, S = cfg->num_slices, K = cfg->num_phantom;
+    okey kc = {k0, k1};
+    okey chain_key = key_fold(kc, 0), seed_key = key_fold(kc, 1);
+    /* m = #live points above the contour (the live set is sorted ascending) */
+    long lo = 0, hi = n;
+    while (lo < hi) {
+        long mid = (lo + hi) >> 1;
+        if (live_L[mid] > Lstar) hi = mid; else lo = mid + 1;
+    }
+    long mm = n - lo, idx = 0;
+    if (mm > 0) {
+        /* resample_indicies (random.py:34-75) in its exact integer form k = ceil(m (1 - U)) */
+        uint64_t M52 = bits64(seed_key, 0) >> 12;
+        uint64_t q = (1ull << 52) - M52;
+        unsigned __int128 prod = (unsigned __int128)(uint64_t)mm * q;
+        uint64_t kk = (uint64_t)(prod >> 52);
+        if ((uint64_t)prod & ((1ull << 52) - 1)) kk += 1;
+        idx = (n - mm) + (long)kk - 1;
+    }
+    float u0[128], d[128];
+    memcpy(u0, live_U + idx * D, sizeof(float) * D);
+    float logL0 = live_L[idx];
+    okey slices_key = key_fold(chain_key, 1);
+    o32_direction(m, key_fold(chain_key, 0), d);
+    long total = 0;
+    for (int j = 0; j < S; ++j) {
+        okey B = key_fold(slices_key, (uint64_t)j);
+        okey ck = key_fold(B, 0), tk = key_fold(B, 2), after = key_fold(B, 3);
+        float alpha = o32_alpha(j, S);
+        int climb = 0;
+        if (cfg->gradient_slice) {
+            /* gradient_slice (uni_slice_sampler.py:202-214) */
+            float g[128], gg = 0.0f;
+            o32_grad_u(m, u0, g);
+            ++total;
+            for (int q = 0; q < D; ++q) gg = fmaf(g[q], g[q], gg);
+            float gn = sqrtf(gg);
+            if (gn != 0.0f && isfinite(gn)) {
+                climb = 1;
+                for (int q = 0; q < D; ++q) d[q] = g[q] / gn;
+            }
+        }
+        /* _slice_bounds (uni_slice_sampler.py:41-64) with one reciprocal per component */
+        float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
+        for (int q = 0; q < D; ++q) {
+            float rc = 1.0f / d[q];
+            float t1 = (1.0f - u0[q]) * rc, t0 = -u0[q] * rc;
+            t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
+            t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
+            t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
+            t0l = fmaxf(t0l, t0 <= 0.f ? t0 : -INFINITY);
+        }
+        float right = fminf(t0r, t1r), left = climb ? 0.0f : fmaxf(t0l, t1l);
+        long in_slice = 0;
+        float t = 0.0f, logL;
+        for (;;) {
+            float u = o32_uniform(tk);
+            t = fmaf(u, right - left, left);
+            logL = o32_loglik_line(m, u0, d, t);
+            ++total;
+            ++in_slice;
+            int accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
+            if (accept || in_slice >= max_evals_per_slice) break;
+            /* _shrink_interval (uni_slice_sampler.py:92-111) and the next pick */
+            okey Bs = ck;
+            ck = key_fold(Bs, 0);
+            tk = key_fold(Bs, 1);
+            if (t < 0.f) left = t;
+            if (t > 0.f) right = t;
+            if (cfg->midpoint_shrink) {
+                if (t < 0.f) left = alpha * left;
+                if (t > 0.f) right = alpha * right;
+            }
+        }
+        for (int q = 0; q < D; ++q) u0[q] = fmaf(t, d[q], u0[q]);
+        logL0 = logL;
+        int p = j - (S - 1 - K);
+        if (K > 0 && p >= 0 && j < S - 1) {
+            memcpy(ph_U + (size_t)p * D, u0, sizeof(float) * D);
+            ph_L[p] = logL;
+        }
+        if (cfg->gradient_guided) {
+            /* Householder reflection at the accepted point (uni_slice_sampler.py:255-269) */
+            ++total;
+            if (j + 1 < S) {
+                float g[128], gg = 0.0f;
+                o32_grad_u(m, u0, g);
+                for (int q = 0; q < D; ++q) gg = fmaf(g[q], g[q], gg);
+                float gn = sqrtf(gg);
+                if (!(gn >= 1e-10f) || isinf(gn)) {
+                    o32_direction(m, key_fold(after, 0), d);
+                } else {
+                    float dot = 0.0f, dd = 0.0f;
+                    for (int q = 0; q < D; ++q) dot = fmaf(d[q], g[q] / gn, dot);
+                    for (int q = 0; q < D; ++q) {
+                        d[q] = fmaf(-2.0f * dot, g[q] / gn, d[q]);
+                        dd = fmaf(d[q], d[q], dd);
+                    }
+                    float dn = sqrtf(dd);
+                    for (int q = 0; q < D; ++q) d[q] = d[q] / dn;
+                }
+            }
+        } else if (j + 1 < S) {
+            o32_direction(m, after, d);
+        }
+    }
+    memcpy(U_out, u0, sizeof(float) * D);
+    *L_out = logL0;
+    *E_out = total;
+}
+
+/* One shell: chains c = 0..num_chains-1 with keys split(sample_key, .)[c] (get_samples,
+ * sharded_static.py:88-129).  ph_U: [num_chains, K, D], ph_L: [num_chains, K] (may be NULL
+ * when K = 0). */
+void orc32_slice_shell(const orc32_model *m, const orc_slice_cfg *cfg, uint32_t k0, uint32_t k1, float Lstar,
+                       const float *live_U, const float *live_L, long n, long num_chains, long max_evals_per_slice,
+                       float *U_out, float *L_out, long *E_out, float *ph_U, float *ph_L) {
+    okey key = {k0, k1};
+    int D = m->D, K = cfg->num_phantom;
+    for (long c = 0; c < num_chains; ++c) {
+        okey kc = key_fold(key, (uint64_t)c);
+        orc32_slice_chain(m, cfg, kc.k0, kc.k1, Lstar, live_U, live_L, n, max_evals_per_slice, U_out + c * D,
+                          &L_out[c], &E_out[c], ph_U ? ph_U + (size_t)c * K * D : NULL,
+                          ph_L ? ph_L + (size_t)c * K : NULL);
+    }
+}
+
+/* The elementary functions of gbns_fmath.h (for their accuracy tests) */
+float orc32_fm_exp(float x) { return gbns_fm_exp(x); }
+float orc32_fm_log(float x) { return gbns_fm_log(x); }
+float orc32_fm_log1p(float x) { return gbns_fm_log1p(x); }
+float orc32_fm_ndtri(float u) { return gbns_fm_ndtri(u); }
+float orc32_fm_ndtri_d(double u) { return gbns_fm_ndtri_d(u); }
+float orc32_fm_normal_from_bits(uint64_t b) { return gbns_fm_normal_from_mantissa(b >> 12); }

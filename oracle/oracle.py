@@ -18,6 +18,9 @@ import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _SRC = os.path.join(_HERE, "ns_oracle.c")
+# the fp32 kernel-arithmetic mode evaluates the product's elementary functions (pure IEEE
+# arithmetic, no device code): a change there rebuilds the oracle
+_FMATH = os.path.join(os.path.dirname(_HERE), "jaxns_gb300", "csrc", "gbns_fmath.h")
 _BUILD = os.path.join(_HERE, "_build")
 _LIB_PATH = os.path.join(_BUILD, "libnsoracle.so")
 
@@ -32,7 +35,7 @@ def build(force: bool = False) -> str:
     """Compile the oracle with gcc (no FMA contraction, IEEE semantics)."""
     os.makedirs(_BUILD, exist_ok=True)
     if (not force and os.path.exists(_LIB_PATH)
-            and os.path.getmtime(_LIB_PATH) >= os.path.getmtime(_SRC)):
+            and os.path.getmtime(_LIB_PATH) >= max(os.path.getmtime(_SRC), os.path.getmtime(_FMATH))):
         return _LIB_PATH
     tmp = _LIB_PATH + f".tmp{os.getpid()}"
     cmd = ["gcc", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
@@ -47,12 +50,14 @@ class _Model(ctypes.Structure):
                 ("prior_kind", ctypes.POINTER(ctypes.c_int)),
                 ("prior_a", ctypes.POINTER(ctypes.c_double)),
                 ("prior_b", ctypes.POINTER(ctypes.c_double)),
-                ("p", ctypes.POINTER(ctypes.c_double)), ("N", ctypes.c_int)]
+                ("p", ctypes.POINTER(ctypes.c_double)), ("N", ctypes.c_int),
+                ("prior_A", ctypes.POINTER(ctypes.c_double)), ("prior_c", ctypes.POINTER(ctypes.c_double))]
 
 
 class _SliceCfg(ctypes.Structure):
     _fields_ = [("num_slices", ctypes.c_int), ("num_phantom", ctypes.c_int),
-                ("midpoint_shrink", ctypes.c_int), ("gradient_guided", ctypes.c_int)]
+                ("midpoint_shrink", ctypes.c_int), ("gradient_guided", ctypes.c_int),
+                ("gradient_slice", ctypes.c_int)]
 
 
 class _NSCfg(ctypes.Structure):
@@ -116,6 +121,14 @@ def lib():
         _lib = ctypes.CDLL(path)
         _lib.orc_ns_run.restype = ctypes.c_long
         _lib.orc_erfinv.restype = ctypes.c_double
+        for nm in ("orc32_fm_exp", "orc32_fm_log", "orc32_fm_log1p", "orc32_fm_ndtri"):
+            getattr(_lib, nm).restype = ctypes.c_float
+            getattr(_lib, nm).argtypes = [ctypes.c_float]
+        _lib.orc32_fm_ndtri_d.restype = ctypes.c_float
+        _lib.orc32_fm_ndtri_d.argtypes = [ctypes.c_double]
+        _lib.orc32_fm_normal_from_bits.restype = ctypes.c_float
+        _lib.orc32_fm_normal_from_bits.argtypes = [ctypes.c_uint64]
+        _lib.orc32_forward.restype = ctypes.c_float
     return _lib
 
 
@@ -192,6 +205,8 @@ class OracleModel:
     prior_b: np.ndarray
     params: np.ndarray
     N: int = 0
+    prior_A: Optional[np.ndarray] = None  # X = A q + c after the per-dimension quantiles q
+    prior_c: Optional[np.ndarray] = None
 
     def _c(self):
         self._keep = [np.ascontiguousarray(self.prior_kind, np.int32),
@@ -199,7 +214,11 @@ class OracleModel:
                       np.ascontiguousarray(self.prior_b, np.float64),
                       np.ascontiguousarray(self.params, np.float64)]
         k, a, b, p = self._keep
-        return _Model(self.D, self.family, _ip(k), _dp(a), _dp(b), _dp(p), self.N)
+        A = c = None
+        if self.prior_A is not None:
+            self._keep += [np.ascontiguousarray(self.prior_A, np.float64), np.ascontiguousarray(self.prior_c, np.float64)]
+            A, c = _dp(self._keep[4]), _dp(self._keep[5])
+        return _Model(self.D, self.family, _ip(k), _dp(a), _dp(b), _dp(p), self.N, A, c)
 
 
 def mvn_model(low, high, mu, cov):
@@ -208,6 +227,16 @@ def mvn_model(low, high, mu, cov):
     params = np.concatenate([np.asarray(mu, np.float64), L.ravel()])
     return OracleModel(D, LIK_MVN, np.zeros(D, np.int32), np.asarray(low, np.float64) * np.ones(D),
                        (np.asarray(high, np.float64) - np.asarray(low, np.float64)) * np.ones(D), params)
+
+
+def mvn_tril_prior_model(prior_loc, prior_L, mu, cov):
+    """Correlated-Gaussian likelihood N(mu, cov) under a MultivariateNormalTriL(prior_loc,
+    prior_L) prior: X = prior_loc + prior_L ndtri(U)."""
+    D = len(mu)
+    L = np.linalg.cholesky(np.asarray(cov, np.float64))
+    params = np.concatenate([np.asarray(mu, np.float64), L.ravel()])
+    return OracleModel(D, LIK_MVN, np.ones(D, np.int32), np.zeros(D), np.ones(D), params,
+                       prior_A=np.tril(np.asarray(prior_L, np.float64)), prior_c=np.asarray(prior_loc, np.float64))
 
 
 def shells_model(low, high, c1, c2, radius, width):
@@ -246,11 +275,11 @@ def grad_U(model, U):
 
 
 def slice_get_sample(model, key, L_star, live_U, live_logL, num_slices, num_phantom=0,
-                     midpoint_shrink=True, gradient_guided=False):
+                     midpoint_shrink=True, gradient_guided=False, gradient_slice=False):
     D = model.D
     live_U = np.ascontiguousarray(live_U, np.float64)
     live_logL = np.ascontiguousarray(live_logL, np.float64)
-    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided))
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided), int(gradient_slice))
     U = np.zeros(D)
     logL = ctypes.c_double()
     ne = ctypes.c_long()
@@ -265,11 +294,11 @@ def slice_get_sample(model, key, L_star, live_U, live_logL, num_slices, num_phan
 
 
 def slice_shell(model, key, L_star, live_U, live_logL, num_chains, num_slices, num_phantom=0,
-                midpoint_shrink=True, gradient_guided=False):
+                midpoint_shrink=True, gradient_guided=False, gradient_slice=False):
     D = model.D
     live_U = np.ascontiguousarray(live_U, np.float64)
     live_logL = np.ascontiguousarray(live_logL, np.float64)
-    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided))
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided), int(gradient_slice))
     U = np.zeros((num_chains, D))
     L = np.zeros(num_chains)
     E = np.zeros(num_chains, np.int64)
@@ -538,3 +567,101 @@ def blr_reweighted(Phi, y, U, log_w, log_tau, log_sigma):
                              ctypes.c_long(U.shape[0]), ctypes.c_double(log_tau), ctypes.c_double(log_sigma),
                              ctypes.byref(lz), _dp(g))
     return lz.value, g
+
+
+# ------------------------------------------------------- fp32 kernel-arithmetic mode
+
+class _Model32(ctypes.Structure):
+    _fields_ = [("D", ctypes.c_int), ("family", ctypes.c_int),
+                ("prior_kind", ctypes.POINTER(ctypes.c_int)),
+                ("prior_a", ctypes.POINTER(ctypes.c_float)),
+                ("prior_b", ctypes.POINTER(ctypes.c_float)),
+                ("p", ctypes.POINTER(ctypes.c_float)), ("variant", ctypes.c_int)]
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+@dataclass
+class Model32:
+    """A model in the device's fp32 tables (prior a/b, the family's parameter vector in the
+    device layout) and the reduction order of the kernel that runs it: variant 0 = one thread
+    per chain, 32 / 64 = the warp-cooperative correlated-Gaussian kernel of that width."""
+    D: int
+    family: int
+    prior_kind: np.ndarray
+    prior_a: np.ndarray
+    prior_b: np.ndarray
+    params: np.ndarray
+    variant: int = 0
+
+    def _c(self):
+        self._keep = [np.ascontiguousarray(self.prior_kind, np.int32),
+                      np.ascontiguousarray(self.prior_a, np.float32),
+                      np.ascontiguousarray(self.prior_b, np.float32),
+                      np.ascontiguousarray(self.params, np.float32)]
+        k, a, b, p = self._keep
+        return _Model32(self.D, self.family, _ip(k), _fp(a), _fp(b), _fp(p), int(self.variant))
+
+
+def kernel_variant(family: int, D: int, warp_min_D: int = 17) -> int:
+    """Which sampler kernel runs a (family, D) run: the correlated-Gaussian family with
+    warp_min_D <= D <= 32 (32) or 32 < D <= 64 (64) runs warp-cooperatively, everything else
+    one thread per chain (0)."""
+    if family == LIK_MVN and D >= warp_min_D:
+        return 32 if D <= 32 else 64
+    return 0
+
+
+def model32(family, D, params, prior_kind, prior_a, prior_b, variant=None, warp_min_D=17):
+    if variant is None:
+        variant = kernel_variant(family, D, warp_min_D)
+    return Model32(D, family, np.asarray(prior_kind, np.int32), np.asarray(prior_a, np.float32),
+                   np.asarray(prior_b, np.float32), np.asarray(params, np.float32), variant)
+
+
+def forward32(model: Model32, U):
+    U = np.ascontiguousarray(np.atleast_2d(U), np.float32)
+    out = np.zeros(U.shape[0], np.float32)
+    m = model._c()
+    lib().orc32_forward_batch(ctypes.byref(m), _fp(U), ctypes.c_long(U.shape[0]), _fp(out))
+    return out
+
+
+def slice_shell32(model: Model32, key, L_star, live_U, live_logL, num_chains, num_slices, num_phantom=0,
+                  midpoint_shrink=True, max_evals_per_slice=100000, gradient_guided=False, gradient_slice=False):
+    """One shell in the kernels' fp32 arithmetic; L_star and live_logL are the device's fp32
+    values (relative to the run's log-likelihood offset)."""
+    D = model.D
+    live_U = np.ascontiguousarray(live_U, np.float32)
+    live_logL = np.ascontiguousarray(live_logL, np.float32)
+    if (gradient_guided or gradient_slice) and model.variant != 0:
+        raise NotImplementedError("the fp32 mode models the gradient options of the thread-per-chain kernel")
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided), int(gradient_slice))
+    U = np.zeros((num_chains, D), np.float32)
+    L = np.zeros(num_chains, np.float32)
+    E = np.zeros(num_chains, np.int64)
+    K = max(num_phantom, 1)
+    pU = np.zeros((num_chains, K, D), np.float32)
+    pL = np.zeros((num_chains, K), np.float32)
+    m = model._c()
+    lib().orc32_slice_shell(ctypes.byref(m), ctypes.byref(cfg), ctypes.c_uint32(int(key[0])),
+                            ctypes.c_uint32(int(key[1])), ctypes.c_float(float(np.float32(L_star))),
+                            _fp(live_U), _fp(live_logL), ctypes.c_long(len(live_logL)), ctypes.c_long(num_chains),
+                            ctypes.c_long(int(max_evals_per_slice)), _fp(U), _fp(L), _lp(E), _fp(pU), _fp(pL))
+    return U, L, E, pU[:, :num_phantom], pL[:, :num_phantom]
+
+
+def fm(name, x):
+    """The product's fp32 elementary function `name` (exp, log, log1p, ndtri, ndtri_d,
+    normal_from_bits) elementwise over x."""
+    f = getattr(lib(), "orc32_fm_" + name)
+    flat = np.ravel(x)
+    if name == "normal_from_bits":
+        vals = [f(ctypes.c_uint64(int(v))) for v in flat]
+    elif name == "ndtri_d":
+        vals = [f(float(v)) for v in flat]
+    else:
+        vals = [f(float(np.float32(v))) for v in flat]
+    return np.array(vals, np.float32).reshape(np.shape(x))
