@@ -41,7 +41,7 @@ __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, co
     const float z1 = (sqrtf(r1) - R) / w, z2 = (sqrtf(r2) - R) / w;
     const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
     const float m = fmaxf(s1, s2), dd = s1 - s2;
-    v = (dd != dd) ? s1 + s2 : m + log1pf(__expf(-fabsf(dd)));
+    v = (dd != dd) ? s1 + s2 : m + gbns_fm_log1p(gbns_fm_exp(-fabsf(dd)));
   } else {
     const int N = rd.N;
     const float *Phi = fp, *y = fp + (size_t)N * D;
@@ -314,7 +314,7 @@ __global__ void k_init_finish(gbns_batch b) {
 
 // _collect_shell (sharded_static.py:210-324) after the chains have run, plus the loop
 // condition of _main_ns_thread (:480-485) and the final live-point append (:833-838).
-__global__ void __launch_bounds__(1024) k_merge(gbns_batch b) {
+__global__ void __launch_bounds__(256) k_merge(gbns_batch b) {
   extern __shared__ unsigned long long sk[];
   __shared__ long long lred[32];
   __shared__ int ired[32];
@@ -387,46 +387,48 @@ __global__ void __launch_bounds__(1024) k_merge(gbns_batch b) {
   for (int i = threadIdx.x; i < n; i += blockDim.x) flat &= (oL[i] == L0);
   flat = cta_and(flat, ired);
 
-  // evidence register (sharded_static.py:284-299) by warp 0
-  if (threadIdx.x < 32) {
-    const double off = rd.log_L_offset;
-    EvAcc acc = evacc_from_shifted(st.ev, off);
-    evidence_scan_warp(acc, L, s, n, 0, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr, off);
-    const gbns_evcalc ev = evacc_to(acc, (double)L[s - 1] + off);
-    evidence_scan_warp(acc, oL, n, 0, n, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr, off);
+  // evidence register (sharded_static.py:284-299): the discarded shell with n live points,
+  // then the remaining live points with n, n-1, ..., 1 (CTA-wide FP64 scans)
+  __shared__ EvScanSmem esm;
+  const double off = rd.log_L_offset;
+  EvAcc acc = evacc_from_shifted(st.ev, off);
+  evidence_scan_cta<false>(acc, L, s, n, 0, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr, off, nullptr, esm);
+  const EvAcc acc_shell = acc;
+  evidence_scan_cta<false>(acc, oL, n, 0, n, nullptr, b.ncoef, b.ncoef_n, nullptr, nullptr, nullptr, off, nullptr,
+                           esm);
+  if (threadIdx.x == 0) {
+    const gbns_evcalc ev = evacc_to(acc_shell, (double)L[s - 1] + off);
     const gbns_evcalc evr = evacc_to(acc, (double)oL[n - 1] + off);
-    if (threadIdx.x == 0) {
-      st.ev = ev;
-      st.ev_rem = evr;
-      st.num_samples += (long long)s * (1 + K);
-      st.next_sample_idx = nsi;
-      st.num_likelihood_evaluations += sumNew;
-      st.log_L_contour = (double)Lstar + off;
-      st.efficiency = (double)n / (double)sumLive;
-      st.plateau = flat;
-      const double Lmin = (double)oL[0] + off, Lmax = (double)oL[n - 1] + off;
-      st.absolute_spread = fabs(Lmax - Lmin);
-      st.relative_spread = 2.0 * st.absolute_spread / fabs(Lmin + Lmax);
-      st.no_seed_points = oL[s - 1] >= oL[n - 1];
-      const double pk = ev.log_X_mean + ev.log_L;
-      st.peak_log_XL = (pk != pk || st.peak_log_XL != st.peak_log_XL) ? NAN : fmax(st.peak_log_XL, pk);
-      // keys: split before the shell (:491), inside _collect_shell (:248), after (:510)
-      const Key K0 = {st.key[0], st.key[1]};
-      const Key k3 = fold(fold(fold(K0, 0u), 0u), 0u);
-      st.key[0] = k3.k0;
-      st.key[1] = k3.k1;
-      st.parity = npar;
-      st.iterations += 1;
-      int reason = 0;
-      bool done = determine_termination(phase_term_cond(rd, 1), st, reason);
-      if (!done && nsi + (long long)s * (1 + K) > rd.cap && !rd.tc.has_max_samples) {
-        // without a sample limit the next shell would overwrite the store
-        atomicOr(&st.status, (int)GBNS_ERR_STORE_FULL);
-        done = true;
-      }
-      st.termination_reason = reason;
-      s_done = done ? 1 : 0;
+    st.ev = ev;
+    st.ev_rem = evr;
+    st.num_samples += (long long)s * (1 + K);
+    st.next_sample_idx = nsi;
+    st.num_likelihood_evaluations += sumNew;
+    st.log_L_contour = (double)Lstar + off;
+    st.efficiency = (double)n / (double)sumLive;
+    st.plateau = flat;
+    const double Lmin = (double)oL[0] + off, Lmax = (double)oL[n - 1] + off;
+    st.absolute_spread = fabs(Lmax - Lmin);
+    st.relative_spread = 2.0 * st.absolute_spread / fabs(Lmin + Lmax);
+    st.no_seed_points = oL[s - 1] >= oL[n - 1];
+    const double pk = ev.log_X_mean + ev.log_L;
+    st.peak_log_XL = (pk != pk || st.peak_log_XL != st.peak_log_XL) ? NAN : fmax(st.peak_log_XL, pk);
+    // keys: split before the shell (:491), inside _collect_shell (:248), after (:510)
+    const Key K0 = {st.key[0], st.key[1]};
+    const Key k3 = fold(fold(fold(K0, 0u), 0u), 0u);
+    st.key[0] = k3.k0;
+    st.key[1] = k3.k1;
+    st.parity = npar;
+    st.iterations += 1;
+    int reason = 0;
+    bool done = determine_termination(phase_term_cond(rd, 1), st, reason);
+    if (!done && nsi + (long long)s * (1 + K) > rd.cap && !rd.tc.has_max_samples) {
+      // without a sample limit the next shell would overwrite the store
+      atomicOr(&st.status, (int)GBNS_ERR_STORE_FULL);
+      done = true;
     }
+    st.termination_reason = reason;
+    s_done = done ? 1 : 0;
   }
   __syncthreads();
   if (s_done) {
@@ -477,9 +479,8 @@ cudaError_t launch_init(const gbns_batch &b, long long total_points, cudaStream_
 cudaError_t launch_merge(const gbns_batch &b, cudaStream_t stream) {
   int NP = 1;
   while (NP < max_n(b)) NP <<= 1;
-  // 256 threads: the FP64 evidence scan runs on one warp while the rest wait at the CTA
-  // barrier, so narrow CTAs let 8 runs' scans share an SM (5.8 % faster on the shells bench
-  // than 1024-thread CTAs)
+  // 256 threads: a run's live set is at most a few thousand points, so narrow CTAs let several
+  // runs' sorts and FP64 scans share an SM
   k_merge<<<b.num_runs, 256, NP * sizeof(unsigned long long), stream>>>(b);
   return cudaGetLastError();
 }

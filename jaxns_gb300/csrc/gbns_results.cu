@@ -100,7 +100,12 @@ __device__ void cta_count_edges(const int *sender, long long N, const unsigned l
   const long long M = N + 1;
   for (long long i = threadIdx.x; i < M; i += blockDim.x) deg[i] = 0;
   __syncthreads();
-  for (long long i = threadIdx.x; i < N; i += blockDim.x) atomicAdd(&deg[max(sender[i], 0)], 1);
+  // out_degree.at[max(sender, 0)].add(1) (tree_structure.py:82-84); like jax's scatter, an
+  // update outside [0, N] is dropped, so a bad sender never writes past the scratch
+  for (long long i = threadIdx.x; i < N; i += blockDim.x) {
+    const int sd = max(sender[i], 0);
+    if ((long long)sd <= N) atomicAdd(&deg[sd], 1);
+  }
   __syncthreads();
   if (threadIdx.x == 0) sm.carry = 1;
   __syncthreads();
@@ -141,14 +146,17 @@ __global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const f
 }
 
 // compute_evidence_stats (internals/shrinkage_statistics.py:131-157) of one sample set on one
-// warp: the final register and the per-sample log X, log dZ and log Z, FP64 (gbns_evidence_stats).
-__global__ void k_evidence_stats(const float *L, const int *nl, long long N, const double *ncoef, int nmax,
-                                 gbns_evcalc *fin, double *lX, double *ldZ, double *lZ) {
+// CTA: the final register and the per-sample log X, log dZ and log Z, FP64 (gbns_evidence_stats).
+template <bool OUT_LZ>
+__global__ void __launch_bounds__(1024) k_evidence_stats(const float *L, const int *nl, long long N, const double *ncoef,
+                                                         int nmax, gbns_evcalc *fin, double *lX, double *ldZ,
+                                                         double *lZ) {
+  __shared__ EvScanSmem esm;
   gbns_evcalc e;
   e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
   e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
   EvAcc acc = evacc_from(e);
-  evidence_scan_warp(acc, L, N, 0, 0, nl, ncoef, nmax, lX, ldZ, lZ);
+  evidence_scan_cta<OUT_LZ>(acc, L, N, 0, 0, nl, ncoef, nmax, lX, ldZ, lZ, 0.0, nullptr, esm);
   if (threadIdx.x == 0) *fin = evacc_to(acc, N > 0 ? (double)L[N - 1] : -INFINITY);
 }
 
@@ -199,14 +207,15 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
   const long long total_evals = cta_sum_ll(ev_sum, lred);
   const long long total_phantom = cta_sum_ll(ph_sum, lred);
   __syncthreads();
-  // evidence statistics (warp 0)
+  // evidence statistics (CTA-wide FP64 scan)
   double *lX = res.log_X_mean + so, *ldp = res.log_dp_mean + so;
-  if (threadIdx.x < 32) {
+  {
+    __shared__ EvScanSmem esm;
     gbns_evcalc e;
     e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
     e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
     EvAcc acc = evacc_from(e);
-    evidence_scan_warp(acc, b.store_L + so, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr, off, si);
+    evidence_scan_cta<false>(acc, b.store_L + so, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr, off, si, esm);
     if (threadIdx.x == 0) {
       const gbns_evcalc f = evacc_to(acc, 0.0);
       s_lz[0] = f.log_Z_mean;
@@ -379,7 +388,8 @@ cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long l
 
 cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream) {
-  k_evidence_stats<<<1, 32, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
+  if (lZ) k_evidence_stats<true><<<1, 1024, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
+  else k_evidence_stats<false><<<1, 1024, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
   return cudaGetLastError();
 }
 

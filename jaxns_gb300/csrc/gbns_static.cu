@@ -36,7 +36,8 @@ void *g_deg_ptr[kMaxDevices] = {nullptr};
 
 // Device addresses of the static scratch on the current device.  The host-side names of the
 // arrays are not device addresses, so they are looked up once per device, with that device
-// current.
+// current.  The cache is keyed by device index only: the addresses are those of the CUDA
+// runtime's primary context, and they do not survive cudaDeviceReset.
 int scratch_for_current_device(void **sort, void **deg) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
