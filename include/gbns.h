@@ -175,7 +175,9 @@ typedef struct {
     int gradient_guided;            /* UniDimSliceSampler(gradient_guided=True): after each accepted point
                                        the direction is reflected about the U-space gradient of log L
                                        (MVN and shells families) */
-    int pad_gg;
+    int gradient_slice;             /* UniDimSliceSampler(gradient_slice=True): every slice runs along the
+                                       normalised U-space gradient at its seed point, t in [0, right]
+                                       (one extra evaluation per slice; MVN and shells families) */
 } gbns_batch;
 
 /* Lock-step chain state of the linear-Gaussian family (device, caller-allocated).  Its
@@ -217,6 +219,16 @@ typedef struct {
     int *tile_pending;                      /* [num_tiles] set by the chain step when a chain of the tile
                                                has a pending proposal; cleared by the residual launch */
     int *tc_done;                           /* [1] CTA completion counter of the residual launch (zeroed) */
+    /* Fused shell (gbns_lg_shell_fused / gbns_lg_iterate): one thread-block cluster of
+     * cluster_size CTAs per (run, 128-chain tile); CTA rank q holds data rows
+     * [q * rows_per_cta, (q + 1) * rows_per_cta) of the run's Phi (TF32 hi / lo) in shared
+     * memory for the whole shell and owns chains q * (128 / cluster_size) ... of the tile. */
+    const int *items_fused;                 /* [num_items_fused * 2]: (run, first chain of the tile) */
+    int num_items_fused;
+    int cluster_size;                       /* 4, 8 or 16 */
+    int rows_per_cta;                       /* 128, 256 or 512; rows_per_cta * ceil(pmax / 32) <= 512 */
+    int pad_fused;
+    long long max_steps;                    /* lock-step budget of one shell (sets GBNS_ERR_SHRINK_BUDGET) */
 } gbns_lg_bufs;
 
 /* results buffers (device) */
@@ -284,7 +296,11 @@ int gbns_count_crossed_edges(const int *sender_dev, const float *log_L_dev, long
  * a deployment that forbids allocation after start-up).  No counterpart in the reference.
  * Scratch is a file-scope device array (5 MiB per device, held until exit) shared by every
  * call: N <= 262143, the first call on a device sets up its address (make it before any
- * stream capture), and calls that overlap on the GPU race. */
+ * stream capture), and calls that overlap on the GPU race.  The address is looked up once per
+ * device index and kept for the life of the process: it belongs to the device's primary
+ * context (the CUDA runtime's), so the entry point is not for callers that run it under a
+ * context of their own, and it must not be called again after cudaDeviceReset (the module's
+ * device memory, and with it the cached address, is gone). */
 int gbns_count_crossed_edges_static(const int *sender_dev, const float *log_L_dev, long long N,
                                     int *samples_indices_dev, int *num_live_points_dev, void *stream);
 /* Linear-Gaussian family: start a shell for every active run (seed points, keys), then
@@ -298,6 +314,21 @@ int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps
  * propose the next point) and the residual contraction of all pending proposals. */
 int gbns_lg_chain_step(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
 int gbns_lg_residual(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
+/* One whole linear-Gaussian shell in one launch: every chain of every active run from its seed
+ * to its last slice (the work of gbns_lg_shell_begin + gbns_lg_steps until chains_left is 0),
+ * with thread-block clusters that keep their share of Phi in shared memory, run the 3xTF32
+ * tcgen05 contraction of each step's proposals and sum the residuals across the cluster in
+ * distributed shared memory (no grid-wide synchronisation, no host round trip).  Needs
+ * gbns_lg_prepare_tc and the fused fields of lg.  Graph-capturable.
+ *   <- get_samples / UniDimSliceSampler.get_sample (sharded_static.py:88-129,
+ *      uni_slice_sampler.py:343-441) for a likelihood evaluated in batches
+ * gbns_lg_iterate: num_iterations x (fused shell + gbns_batch_merge)
+ *   <- the _main_ns_thread loop body (sharded_static.py:487-555) */
+int gbns_lg_shell_fused(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream);
+int gbns_lg_iterate(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_iterations, void *stream);
+/* How many clusters of lg's fused configuration the current device holds at once (0: the
+ * configuration cannot launch here; choose a smaller cluster).  No reference counterpart. */
+int gbns_lg_fused_max_clusters(const gbns_batch *batch, const gbns_lg_bufs *lg, int *max_clusters);
 /* Split each run's Phi (fparams) into the TF32 hi/lo row-padded copies lg->Phi_hi / Phi_lo
  * read by the tensor-core residual path.  Call once per batch, before the first step (and
  * after new parameters). */

@@ -61,7 +61,7 @@ class Batch(ctypes.Structure):
                 ("prior_a", c_void_p), ("prior_b", c_void_p), ("ncoef", c_void_p), ("items", c_void_p),
                 ("num_items", c_int), ("bucket_begin", c_int * 8), ("bucket_end", c_int * 8),
                 ("chains_per_item", c_int), ("max_evals_per_slice", c_int), ("gradient_guided", c_int),
-                ("pad_gg", c_int)]
+                ("gradient_slice", c_int)]
 
 
 class LGBufs(ctypes.Structure):
@@ -73,7 +73,9 @@ class LGBufs(ctypes.Structure):
                 ("use_tc", c_int), ("num_items_tc", c_int), ("items_tc", c_void_p), ("W_hi", c_void_p),
                 ("W_lo", c_void_p), ("Phi_hi", c_void_p), ("Phi_lo", c_void_p),
                 ("row_base", c_void_p), ("total_rows", c_ll), ("num_ctas_tc", c_int), ("num_tiles", c_int),
-                ("chain_run", c_void_p), ("tile_base", c_void_p), ("tile_pending", c_void_p), ("tc_done", c_void_p)]
+                ("chain_run", c_void_p), ("tile_base", c_void_p), ("tile_pending", c_void_p), ("tc_done", c_void_p),
+                ("items_fused", c_void_p), ("num_items_fused", c_int), ("cluster_size", c_int),
+                ("rows_per_cta", c_int), ("pad_fused", c_int), ("max_steps", c_ll)]
 
 
 class ResultsBufs(ctypes.Structure):
@@ -88,7 +90,7 @@ EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2
             "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
             "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint",
             "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc", "gbns_lg_chain_step", "gbns_lg_residual",
-            "gbns_sample_evidence")
+            "gbns_sample_evidence", "gbns_lg_shell_fused", "gbns_lg_iterate", "gbns_lg_fused_max_clusters")
 
 _lib = None
 

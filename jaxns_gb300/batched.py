@@ -19,7 +19,8 @@ from .public import NestedSampler, NestedSamplerResults, TerminationCondition, r
 class BatchedNestedSampler:
     def __init__(self, samplers: Sequence[NestedSampler], keys, term_conds: Optional[Sequence] = None,
                  block: int = 16, chains_per_item: int = 64, store_U: bool = False, lg_tensor_cores: bool = True,
-                 autotune: bool = False, wide_chains_per_item: int = 0, device="cuda"):
+                 autotune: bool = False, wide_chains_per_item: int = 0, device="cuda", chains_per_lane: int = 1,
+                 warp_min_D: int = 17):
         self.samplers = list(samplers)
         keys = np.asarray(keys, np.uint32).reshape(len(self.samplers), 2)
         if term_conds is None:
@@ -34,11 +35,14 @@ class BatchedNestedSampler:
         if autotune and not any(s.family == FAMILY_LINGAUSS for s in specs):
             # launch shapes timed on this batch (results do not depend on them)
             from .autotune import autotune_launch
-            self.tuning = autotune_launch(specs)
+            self.tuning = autotune_launch(specs, device=device)
             chains_per_item = self.tuning["chains_per_item"]
+            chains_per_lane = self.tuning["chains_per_lane"]
             wide_chains_per_item = self.tuning["wide_chains_per_item"]
+            warp_min_D = self.tuning["warp_min_D"]
         self.batch = NSBatch(specs, device=device, chains_per_item=chains_per_item,
-                             wide_chains_per_item=wide_chains_per_item, lg_tensor_cores=lg_tensor_cores)
+                             wide_chains_per_item=wide_chains_per_item, lg_tensor_cores=lg_tensor_cores,
+                             chains_per_lane=chains_per_lane, warp_min_D=warp_min_D)
         self.state = None
 
     def __call__(self, from_host: bool = True, use_graph: bool = True, check: bool = True,

@@ -23,6 +23,8 @@ cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cuda
 cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t stream);
 cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
+cudaError_t launch_lg_shell_fused(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
+cudaError_t lg_fused_max_clusters(const gbns_lg_bufs &lg, int *out);
 cudaError_t launch_adjoint_reduce(const double *log_w, long long M, int N, double log_sigma, const double *ss,
                                   const double *ry, double *out, cudaStream_t stream);
 cudaError_t launch_adjoint_tc(const double *U, const double *log_w, long long M, int P, const float *Phi,

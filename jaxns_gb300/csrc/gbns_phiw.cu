@@ -18,51 +18,9 @@
 #include <cstdio>
 #include "gbns_device.cuh"
 #include "gbns_launch.h"
+#include "gbns_lg.cuh"
 
 namespace gbns {
-
-// fp32 pair <-> FP64
-__device__ __forceinline__ void pair_from_double(double u, float &a, float &b) {
-  a = (float)u;
-  b = (float)(u - (double)a);
-}
-
-// a + b as an fp32 pair (TwoSum: exact for any magnitudes).
-__device__ __forceinline__ void pair_add(float a, float s, float &hi, float &lo) {
-  hi = a + s;
-  const float bb = hi - a;
-  lo = (a - (hi - bb)) + (s - bb);
-}
-
-// Standard-normal quantile of u = a + s, in fp32 with the tail argument formed exactly.
-__device__ __forceinline__ float ndtri_pair(float a, float s) {
-  const float z = fmaf(2.0f, a, -1.0f) + 2.0f * s;  // 2u - 1 (2a - 1 exact for a in [1/4, 1])
-  if (fabsf(z) < 0.5f) return GBNS_SQRT2F * erfinvf(z);
-  if (a >= 0.5f) return GBNS_SQRT2F * erfcinvf(2.0f * ((1.0f - a) - s));
-  return -GBNS_SQRT2F * erfcinvf(2.0f * (a + s));
-}
-
-__device__ __forceinline__ float prior_quantile_pair(int kind, float pa, float pb, float a, float s) {
-  if (kind == GBNS_PRIOR_UNIFORM) return fmaf(pb, a, fmaf(pb, s, pa));
-  return fmaf(pb, ndtri_pair(a, s), pa);
-}
-
-__device__ __forceinline__ int run_of_chain(const gbns_batch &b, long long g) {
-  int lo = 0, hi = b.num_runs;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (b.runs[mid].shell_off <= g) lo = mid; else hi = mid;
-  }
-  return lo;
-}
-
-// linspace(0.5, 1, S)[j] (the midpoint shrink factors, uni_slice_sampler.py:114-273).
-__device__ __forceinline__ float lg_alpha(int j, int S) {
-  if (S == 1) return 0.5f;
-  if (j == S - 1) return 1.0f;
-  const float step = (float)j / (float)(S - 1);
-  return 0.5f * (1.0f - step) + step;
-}
 
 // A chain's first state of the shell: seed point (resample_indicies over log L > L*),
 // direction and slice keys (get_sample_from_seed, uni_slice_sampler.py:403-423).

@@ -17,6 +17,7 @@
 #include <mutex>
 #include "gbns_device.cuh"
 #include "gbns_launch.h"
+#include "gbns_lg.cuh"
 
 namespace gbns {
 
@@ -515,6 +516,408 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
   }
 }
 
+
+// ------------------------------------------------------------------ fused shell
+//
+// One whole lock-step shell of the linear-Gaussian family in one launch.  A thread-block
+// cluster of CS CTAs owns one (run, 128-chain tile).  CTA rank q keeps data rows
+// [q R, (q + 1) R) of the run's Phi (TF32 hi / lo, K-major 128B-swizzled, loaded once by TMA)
+// in shared memory for the whole shell, a 128-chain x R-row accumulator in tensor memory, and
+// owns chains q (128 / CS) ... of the tile: one warp per chain, lanes over dimensions, the
+// chain logic of k_lg_step with the chain state in registers.  A step:
+//   1. every owner warp consumes its chain's residual sum, advances the slice logic and writes
+//      the chain's next proposal (one TF32 hi / lo row) into the W tile of every CTA of the
+//      cluster (distributed shared memory);
+//   2. cluster barrier; the CTAs' counts of active chains travel with it, and the cluster
+//      leaves the loop when none is left;
+//   3. one thread issues the 3xTF32 tcgen05 MMAs of W (128 chains) x Phi slice (R rows);
+//   4. every warp drains a lane quarter x column slice of the accumulator (thread = chain),
+//      sums (y - Phi w)^2 over its rows and stores the partial sum in the owner CTA's shared
+//      memory; cluster barrier.
+// The owner adds a chain's partial sums in rank order, so the sum is deterministic.  Every
+// mbarrier wait is bounded: a CTA whose wait timed out reports it through its active count,
+// every CTA of the cluster then leaves at the same barrier, and the run's status gets
+// GBNS_ERR_WAIT_TIMEOUT.
+
+struct LfArgs {
+  int cs;    // cluster size (CTAs per chain tile)
+  int rows;  // data rows per CTA (R)
+  int nkb;   // K blocks of 32 floats
+  int cpc;   // chains per CTA = warps per CTA (128 / cs)
+};
+
+struct alignas(128) LfMaps {
+  CUtensorMap phi_hi, phi_lo;
+};
+
+__device__ __forceinline__ uint32_t lf_cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void lf_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// shared::cluster address of the same variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t lf_mapa(uint32_t saddr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(saddr), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void lf_st_v4(uint32_t addr, uint4 v) {
+  asm volatile("st.shared::cluster.v4.u32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "r"(v.x), "r"(v.y), "r"(v.z), "r"(v.w)
+               : "memory");
+}
+
+__device__ __forceinline__ void lf_st_f64(uint32_t addr, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+}
+
+__device__ __forceinline__ void lf_st_s32(uint32_t addr, int v) {
+  asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+// byte offset of float k (0..31) of row `row` in a K-major tile with the 128-byte swizzle
+// that TMA writes: the 16-byte chunk index is xor-ed with the row's position in its 8-row group
+__device__ __forceinline__ uint32_t lf_sw128(int row, int k) {
+  return (uint32_t)row * 128u + ((((uint32_t)k >> 2) ^ ((uint32_t)row & 7u)) << 4) + (((uint32_t)k & 3u) << 2);
+}
+
+constexpr int LF_ABORT = -(1 << 24);
+constexpr int LF_M_TILE = 128;  // chains per cluster tile (tensor-memory lanes)
+
+__global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ LfMaps maps, gbns_batch b,
+                                                        gbns_lg_bufs lg, LfArgs la) {
+  extern __shared__ unsigned char lf_dyn[];
+  __shared__ __align__(8) unsigned long long bars[2];  // 0: Phi slice landed, 1: MMAs of a step done
+  __shared__ uint32_t tmem_slot;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int CS = la.cs, R = la.rows, NKB = la.nkb, CPC = la.cpc, H = la.cpc / 4;
+  const uint32_t rank = lf_cluster_rank();
+  const int cl = blockIdx.x / CS;
+  const int r = lg.items_fused[2 * cl], tile_c0 = lg.items_fused[2 * cl + 1];
+  const gbns_run_desc &rd = b.runs[r];
+  gbns_run_state &st = b.state[r];
+  if (st.done || st.phase != 1) return;  // the same answer in every CTA of the cluster
+  const int P = rd.D, N = rd.N, S = rd.S, K = rd.K, s = rd.s, n = rd.n;
+  const int row0 = (int)rank * R;
+  const int nrows = max(0, min(R, N - row0));
+
+  // ---- shared memory: Phi slice (hi, lo), W tile (hi, lo), y slice, partial sums, counts
+  const uint32_t dyn0 = smem_u32(lf_dyn);
+  const uint32_t base = (dyn0 + 1023u) & ~1023u;
+  const uint32_t phi_hi = base, phi_lo = base + (uint32_t)(NKB * R * 128);
+  const uint32_t w_hi = base + (uint32_t)(2 * NKB * R * 128), w_lo = w_hi + (uint32_t)(NKB * 16384);
+  const uint32_t ys_s = w_lo + (uint32_t)(NKB * 16384);
+  const uint32_t slots_s = ys_s + (uint32_t)(R * 4);                  // double [CS][H][CPC]
+  const uint32_t active_s = slots_s + (uint32_t)(CS * H * CPC * 8);   // int [CS]
+  auto gptr = [&](uint32_t sa) { return (void *)(lf_dyn + (sa - dyn0)); };
+  float *ys = (float *)gptr(ys_s);
+  const double *slots = (const double *)gptr(slots_s);
+  const int *active_in = (const int *)gptr(active_s);
+  const uint32_t bar_phi = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+
+  if (tid == 0) {
+    mbar_init(bar_phi, 1);
+    mbar_init(bar_mma, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_slot)),
+                 "r"((uint32_t)R)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  // W tile zeroed (dimensions >= P stay zero); y slice
+  for (uint32_t q = (uint32_t)tid; q < (uint32_t)(NKB * 2048); q += blockDim.x)
+    *(uint4 *)gptr(w_hi + 16u * q) = make_uint4(0u, 0u, 0u, 0u);
+  const float *yrun = b.fparams + rd.param_off + (size_t)N * P;
+  for (int q = tid; q < R; q += blockDim.x) ys[q] = q < nrows ? yrun[row0 + q] : 0.0f;
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot;
+  const int nbox = (nrows + 127) >> 7;
+  if (tid == 0 && nbox > 0) {
+    mbar_expect_tx(bar_phi, (uint32_t)(2 * NKB * nbox) * SR_BOX);
+    const int brow = (int)lg.row_base[r] + row0;
+    for (int kb = 0; kb < NKB; ++kb)
+      for (int i = 0; i < nbox; ++i) {
+        const uint32_t o = (uint32_t)(kb * R * 128 + i * 16384);
+        tma_load_2d(phi_hi + o, &maps.phi_hi, kb * TC_KB, brow + 128 * i, bar_phi);
+        tma_load_2d(phi_lo + o, &maps.phi_lo, kb * TC_KB, brow + 128 * i, bar_phi);
+      }
+  }
+  int abort_local = 0;
+  if (nbox > 0) abort_local = __syncthreads_or(!mbar_wait(bar_phi, 0)) ? 1 : 0;
+
+  // ---- the owned chain (warp): seed point, keys (k_lg_init)
+  const float *liveL = b.live_L[st.parity] + rd.live_off;
+  const float Lstar = liveL[rd.s - 1];
+  const int crow = (int)rank * CPC + warp;  // chain row in the tile
+  const int c = tile_c0 + crow;
+  const int pa_ = lane, pb_ = lane + 32;
+  const bool ha = pa_ < P, hb = pb_ < P;
+  int flags = LG_DONE;
+  float ua = 0.f, la_ = 0.f, ub = 0.f, lb = 0.f, da = 0.f, db = 0.f;
+  int j = 0, total = 0, in_slice = 0;
+  float left = 0.f, right = 0.f, t = 0.f, alpha = 0.5f, logL0 = 0.f;
+  Key ck = {0u, 0u}, after_key = {0u, 0u}, dir_key = {0u, 0u}, slices_key = {0u, 0u};
+  if (c < s) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (liveL[mid] > Lstar) hi = mid; else lo = mid + 1;
+    }
+    const int m = n - lo;
+    const Key k0 = {st.key[0], st.key[1]};
+    const Key sample_key = fold(fold(k0, 0u), 1u);
+    const Key kc = fold(sample_key, (uint32_t)c);
+    const Key chain_key = fold(kc, 0u), seed_key = fold(kc, 1u);
+    int idx = 0;
+    if (m > 0) {
+      const uint64_t M52 = bits64(seed_key, 0u) >> 12;
+      const uint64_t q = (1ull << 52) - M52;
+      const uint64_t lo64 = (uint64_t)m * q, hi64 = __umul64hi((uint64_t)m, q);
+      uint64_t kk = (hi64 << 12) | (lo64 >> 52);
+      if (lo64 & ((1ull << 52) - 1)) kk += 1;
+      idx = (n - m) + (int)kk - 1;
+    }
+    const double *liveU = (const double *)(b.live_U[st.parity] + rd.liveU_off);
+    if (ha) pair_from_double(liveU[(size_t)idx * P + pa_], ua, la_);
+    if (hb) pair_from_double(liveU[(size_t)idx * P + pb_], ub, lb);
+    logL0 = liveL[idx];
+    dir_key = fold(chain_key, 0u);
+    slices_key = fold(chain_key, 1u);
+    flags = LG_START | LG_NEED_DIR;
+  }
+  const float *fp = b.fparams + rd.param_off;
+  const float sigma = fp[(size_t)N * P + N];
+  const float inv2s2 = 0.5f / (sigma * sigma);
+  const int *kind = b.prior_kind + rd.prior_off;
+  const float *pra = b.prior_a + rd.prior_off, *prb = b.prior_b + rd.prior_off;
+  lf_cluster_sync();  // every CTA initialised before the first remote store
+
+  const int NMMA = R < 256 ? R : 256;
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NMMA >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+  const int nk8 = (P + 7) >> 3;
+  const int qd = warp & 3, hs = warp >> 2;  // accumulator lane quarter and column slice of this warp
+  uint32_t mma_phase = 0;
+  bool mma_pending = false;
+  for (long long step = 0;; ++step) {
+    // ---- 1. chain step of the owned chain (k_lg_step)
+    bool wrote = false;
+    if (!(flags & LG_DONE)) {
+      if (flags & LG_PENDING) {
+        double ss = 0.0;
+        if (lane == 0)
+          for (int src = 0; src < CS; ++src)
+            for (int h = 0; h < H; ++h) ss += slots[(src * H + h) * CPC + warp];
+        ss = __shfl_sync(0xffffffffu, ss, 0);
+        float logL = (float)(-ss * (double)inv2s2);  // relative to the run's log_L_offset
+        if (logL != logL) logL = -INFINITY;
+        ++total;
+        ++in_slice;
+        const bool accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
+        if (accept || in_slice >= b.max_evals_per_slice) {
+          if (!accept) flags |= LG_FAILED;
+          pair_add(ua, fmaf(t, da, la_), ua, la_);
+          pair_add(ub, fmaf(t, db, lb), ub, lb);
+          logL0 = logL;
+          const int ph = j - (S - 1 - K);
+          if (K > 0 && ph >= 0 && j < S - 1) {
+            double *phU = (double *)(b.ph_U + rd.phU_off) + ((size_t)c * K + ph) * P;
+            if (ha) phU[pa_] = (double)ua + (double)la_;
+            if (hb) phU[pb_] = (double)ub + (double)lb;
+            if (lane == 0) b.ph_L[rd.phL_off + (size_t)c * K + ph] = logL;
+          }
+          ++j;
+          flags |= LG_START;
+          if (j < S) {
+            flags |= LG_NEED_DIR;
+            dir_key = after_key;
+          } else {
+            flags |= LG_DONE;
+          }
+        } else {
+          flags &= ~LG_START;
+        }
+        flags &= ~LG_PENDING;
+      }
+      if (flags & LG_DONE) {
+        double *nu = (double *)(b.new_U + rd.newU_off) + (size_t)c * P;
+        if (ha) nu[pa_] = (double)ua + (double)la_;
+        if (hb) nu[pb_] = (double)ub + (double)lb;
+        if (lane == 0) {
+          b.new_L[rd.shell_off + c] = logL0;
+          b.new_E[rd.shell_off + c] = total;
+          if (flags & LG_FAILED) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
+        }
+      } else {
+        if (flags & LG_NEED_DIR) {
+          if (P == 1) {
+            da = 1.0f;
+          } else {
+            const float va = ha ? normal_from_bits(bits64(dir_key, (uint32_t)pa_)) : 0.0f;
+            const float vb = hb ? normal_from_bits(bits64(dir_key, (uint32_t)pb_)) : 0.0f;
+            const float nrm = sqrtf(warp_sum(fmaf(va, va, vb * vb)));
+            da = va / nrm;
+            db = vb / nrm;
+          }
+          flags &= ~LG_NEED_DIR;
+        }
+        const bool start = (flags & LG_START) != 0;
+        const Key B = start ? fold(slices_key, (uint32_t)j) : ck;
+        ck = fold(B, 0u);
+        const Key tk = fold(B, start ? 2u : 1u);
+        if (start) {
+          after_key = fold(B, 3u);
+          alpha = lg_alpha(j, S);
+          float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const bool have = h ? hb : ha;
+            if (have) {
+              const float uu = h ? ub : ua, ll = h ? lb : la_, dd = h ? db : da;
+              const float t1 = ((1.0f - uu) - ll) / dd, t0 = -(uu + ll) / dd;
+              t1r = fminf(t1r, t1 >= 0.f ? t1 : INFINITY);
+              t1l = fmaxf(t1l, t1 <= 0.f ? t1 : -INFINITY);
+              t0r = fminf(t0r, t0 >= 0.f ? t0 : INFINITY);
+              t0l = fmaxf(t0l, t0 <= 0.f ? t0 : -INFINITY);
+            }
+          }
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            t1r = fminf(t1r, __shfl_xor_sync(0xffffffffu, t1r, o));
+            t1l = fmaxf(t1l, __shfl_xor_sync(0xffffffffu, t1l, o));
+            t0r = fminf(t0r, __shfl_xor_sync(0xffffffffu, t0r, o));
+            t0l = fmaxf(t0l, __shfl_xor_sync(0xffffffffu, t0l, o));
+          }
+          right = fminf(t0r, t1r);
+          left = fmaxf(t0l, t1l);
+          in_slice = 0;
+        } else {
+          if (t < 0.f) left = t;
+          if (t > 0.f) right = t;
+          if (rd.midpoint) {
+            if (t < 0.f) left = alpha * left;
+            if (t > 0.f) right = alpha * right;
+          }
+        }
+        t = fmaf(uniform01(bits64(tk, 0u)), right - left, left);
+        // the proposal w as a TF32 hi / lo row of the W tile
+        if (ha) {
+          const float w = prior_quantile_pair(kind[pa_], pra[pa_], prb[pa_], ua, fmaf(t, da, la_));
+          float h, l;
+          tf32_split(w, h, l);
+          *(float *)gptr(w_hi + lf_sw128(crow, pa_)) = h;
+          *(float *)gptr(w_lo + lf_sw128(crow, pa_)) = l;
+        }
+        if (hb) {
+          const float w = prior_quantile_pair(kind[pb_], pra[pb_], prb[pb_], ub, fmaf(t, db, lb));
+          float h, l;
+          tf32_split(w, h, l);
+          *(float *)gptr(w_hi + 16384u + lf_sw128(crow, lane)) = h;
+          *(float *)gptr(w_lo + 16384u + lf_sw128(crow, lane)) = l;
+        }
+        flags |= LG_PENDING;
+        wrote = true;
+      }
+    }
+    __syncwarp();
+    if (wrote && lane < 16 * NKB) {
+      // copy the row (hi and lo, NKB blocks of 128 bytes) to the other CTAs of the cluster
+      const int blk = lane >> 3, chunk = lane & 7;
+      const uint32_t off = ((blk & 1) ? w_lo : w_hi) + (uint32_t)(blk >> 1) * 16384u + (uint32_t)crow * 128u +
+                           (uint32_t)chunk * 16u;
+      const uint4 v = *(const uint4 *)gptr(off);
+      for (int q = 0; q < CS; ++q)
+        if (q != (int)rank) lf_st_v4(lf_mapa(off, (uint32_t)q), v);
+    }
+    asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
+    const int act = __syncthreads_count(lane == 0 && !(flags & LG_DONE));
+    if (tid < CS) lf_st_s32(lf_mapa(active_s + 4u * rank, (uint32_t)tid), abort_local ? LF_ABORT : act);
+    lf_cluster_sync();  // (A) W tiles and active counts complete in every CTA
+    int total_active = 0;
+    for (int q = 0; q < CS; ++q) total_active += active_in[q];
+    if (total_active <= 0 || step >= lg.max_steps) {
+      if (tid == 0 && rank == 0) {
+        if (total_active < 0) atomicOr(&st.status, (int)GBNS_ERR_WAIT_TIMEOUT);
+        else if (total_active > 0) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
+      }
+      break;
+    }
+    // ---- 2. 3xTF32 MMAs: accumulator[chain][row] = W[chain] . Phi[row] over this CTA's rows
+    if (nbox > 0 && tid == 0) {
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc_fence_after();
+      for (int nc = 0; nc * NMMA < nbox * 128; ++nc) {
+        const uint32_t d = tmem + (uint32_t)(nc * NMMA);
+        for (int k8 = 0; k8 < nk8; ++k8) {
+          const int kb = k8 >> 2;
+          const uint32_t koff = (uint32_t)(k8 & 3) * 32u;
+          const uint32_t wo = (uint32_t)kb * 16384u + koff;
+          const uint32_t po = (uint32_t)(kb * R * 128 + nc * NMMA * 128) + koff;
+          const uint64_t ah = smem_desc(w_hi + wo), al = smem_desc(w_lo + wo);
+          const uint64_t bh = smem_desc(phi_hi + po), bl = smem_desc(phi_lo + po);
+          tc_mma_d(d, al, bh, idesc, k8 > 0 ? 1u : 0u);
+          tc_mma_d(d, ah, bl, idesc, 1u);
+          tc_mma_d(d, ah, bh, idesc, 1u);
+        }
+      }
+      tc_commit(bar_mma);
+    }
+    // ---- 3. epilogue: this warp's 32 chains x its column slice
+    double part = 0.0;
+    if (nbox > 0) {
+      bool ok = mbar_wait(bar_mma, mma_phase);
+      ok = __syncthreads_and(ok);
+      if (!ok) {
+        abort_local = 1;
+        mma_pending = true;  // the phase stays the one still owed
+      } else {
+        mma_phase ^= 1u;
+        tc_fence_after();
+        const int cw = R / H;
+        const int cbeg = hs * cw, cend = min(cbeg + cw, nrows);
+        const uint32_t taddr = tmem + ((uint32_t)(qd * 32) << 16);
+        for (int col = cbeg; col < cend; col += 32) {
+          float v[32];
+          tc_ld32(taddr + (uint32_t)col, v);
+          float p = 0.0f;
+#pragma unroll
+          for (int q = 0; q < 32; ++q) {
+            const float rr = ys[col + q] - v[q];
+            p = (col + q < cend) ? fmaf(rr, rr, p) : p;
+          }
+          part += (double)p;
+        }
+      }
+    }
+    {
+      const int row_c = qd * 32 + lane;  // chain row of this thread's accumulator lane
+      const int owner = row_c / CPC, lc = row_c - owner * CPC;
+      lf_st_f64(lf_mapa(slots_s + 8u * (uint32_t)(((int)rank * H + hs) * CPC + lc), (uint32_t)owner), part);
+    }
+    tc_fence_before();
+    lf_cluster_sync();  // (B) partial sums complete in their owners
+  }
+  // a timed-out MMA may still be in flight: give it one more bounded wait before the
+  // tensor memory is released
+  if (mma_pending && tid == 0) mbar_wait(bar_mma, mma_phase);
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)R) : "memory");
+  }
+  lf_cluster_sync();
+}
+
 // Adjoint: all dead points (blockIdx.x: 128-point tile) against all rows (blockIdx.y).
 __global__ void __launch_bounds__(128) k_adj_resid_tc(const __grid_constant__ TcMaps maps, long long M, int P, int N,
                                                       const float *y, double *ss, double *ry, int *status) {
@@ -672,6 +1075,70 @@ cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int 
   return cudaGetLastError();
 }
 
+
+// Launch configuration of the fused shell: clusters of lg.cluster_size CTAs over lg.items_fused.
+static cudaError_t lf_config(const gbns_lg_bufs &lg, cudaStream_t s, cudaLaunchConfig_t &cfg, cudaLaunchAttribute *attr,
+                             LfArgs &la) {
+  const int cs = lg.cluster_size, R = lg.rows_per_cta, nkb = lg.pmax > TC_KB ? 2 : 1;
+  if ((cs != 8 && cs != 16) || (R != 128 && R != 256 && R != 512) || nkb * R > 512 || lg.num_items_fused < 1 ||
+      !lg.items_fused)
+    return cudaErrorInvalidValue;
+  const int cpc = LF_M_TILE / cs;
+  // Phi slice and W tile (hi, lo), y slice, partial sums, counts; at least 1/(512/R + 1) of an
+  // SM's shared memory, so that the CTAs resident on one SM never ask for more than its 512
+  // tensor-memory columns (an allocation that has to wait could stall a cluster barrier)
+  size_t smem = 1024 + (size_t)2 * nkb * R * 128 + (size_t)2 * nkb * 16384 + (size_t)R * 4 +
+                (size_t)cs * (cpc / 4) * cpc * 8 + (size_t)cs * 4;
+  const size_t per_sm = 233472, floor_bytes = per_sm / (size_t)(512 / R + 1) + 1;
+  if (smem < floor_bytes) smem = floor_bytes;
+  if (smem > 232448) return cudaErrorInvalidValue;
+  cudaError_t e = cudaFuncSetAttribute(k_lg_shell_fused, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess && cs > 8)
+    e = cudaFuncSetAttribute(k_lg_shell_fused, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if (e != cudaSuccess) return e;
+  cfg = cudaLaunchConfig_t{};
+  cfg.gridDim = dim3((unsigned)(lg.num_items_fused * cs));
+  cfg.blockDim = dim3((unsigned)(32 * cpc));
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cs;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  la.cs = cs;
+  la.rows = R;
+  la.nkb = nkb;
+  la.cpc = cpc;
+  return cudaSuccess;
+}
+
+cudaError_t launch_lg_shell_fused(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute attr[1];
+  LfArgs la;
+  cudaError_t e = lf_config(lg, s, cfg, attr, la);
+  if (e != cudaSuccess) return e;
+  LfMaps maps;
+  if (!encode_rows(&maps.phi_hi, lg.Phi_hi, lg.total_rows, 64, 128) ||
+      !encode_rows(&maps.phi_lo, lg.Phi_lo, lg.total_rows, 64, 128))
+    return cudaErrorInvalidValue;
+  e = cudaLaunchKernelEx(&cfg, k_lg_shell_fused, maps, b, lg, la);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+// Clusters of this configuration that the device can hold at once (0: it cannot launch).
+cudaError_t lg_fused_max_clusters(const gbns_lg_bufs &lg, int *out) {
+  cudaLaunchConfig_t cfg;
+  cudaLaunchAttribute attr[1];
+  LfArgs la;
+  cudaError_t e = lf_config(lg, 0, cfg, attr, la);
+  if (e != cudaSuccess) return e;
+  return cudaOccupancyMaxActiveClusters(out, k_lg_shell_fused, &cfg);
+}
+
 cudaError_t launch_adjoint_tc(const double *U, const double *log_w, long long M, int P, const float *Phi, const float *y,
                               int N, double log_tau, double log_sigma, double *out, double *ss, double *ry,
                               float *w_scratch, float *phi_scratch, int *status, cudaStream_t s) {
@@ -706,6 +1173,56 @@ int tc_fail(int code, const char *msg) {
 }  // namespace
 
 extern "C" {
+
+namespace {
+int fused_check(const gbns_batch *batch, const gbns_lg_bufs *lg, const char *who) {
+  char msg[256];
+  if (!batch || !lg || batch->num_runs <= 0 || lg->pmax < 1 || lg->pmax > 64 || !lg->Phi_hi || !lg->Phi_lo ||
+      !lg->row_base || lg->total_rows < 1 || !lg->items_fused || lg->num_items_fused < 1) {
+    std::snprintf(msg, sizeof msg, "%s: bad arguments (Phi_hi, Phi_lo, row_base, items_fused and 1 <= pmax <= 64 "
+                  "required)", who);
+    return tc_fail(-1, msg);
+  }
+  const int R = lg->rows_per_cta, nkb = lg->pmax > 32 ? 2 : 1;
+  if ((lg->cluster_size != 8 && lg->cluster_size != 16) || (R != 128 && R != 256 && R != 512) || nkb * R > 512 ||
+      lg->max_steps < 1) {
+    std::snprintf(msg, sizeof msg, "%s: cluster_size must be 8 or 16, rows_per_cta 128, 256 or 512 with "
+                  "rows_per_cta * ceil(pmax / 32) <= 512, max_steps >= 1", who);
+    return tc_fail(-1, msg);
+  }
+  return 0;
+}
+}  // namespace
+
+int gbns_lg_shell_fused(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
+  int rc = fused_check(batch, lg, "gbns_lg_shell_fused");
+  if (rc) return rc;
+  cudaError_t e = gbns::launch_lg_shell_fused(*batch, *lg, (cudaStream_t)stream);
+  if (e != cudaSuccess) return tc_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+int gbns_lg_fused_max_clusters(const gbns_batch *batch, const gbns_lg_bufs *lg, int *max_clusters) {
+  int rc = fused_check(batch, lg, "gbns_lg_fused_max_clusters");
+  if (rc) return rc;
+  if (!max_clusters) return tc_fail(-1, "gbns_lg_fused_max_clusters: NULL output");
+  *max_clusters = 0;
+  cudaError_t e = gbns::lg_fused_max_clusters(*lg, max_clusters);
+  if (e != cudaSuccess) return tc_fail(-2, cudaGetErrorString(e));
+  return 0;
+}
+
+int gbns_lg_iterate(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_iterations, void *stream) {
+  int rc = fused_check(batch, lg, "gbns_lg_iterate");
+  if (rc) return rc;
+  if (num_iterations < 0) return tc_fail(-1, "gbns_lg_iterate: negative iteration count");
+  for (int k = 0; k < num_iterations; ++k) {
+    cudaError_t e = gbns::launch_lg_shell_fused(*batch, *lg, (cudaStream_t)stream);
+    if (e == cudaSuccess) e = gbns::launch_merge(*batch, (cudaStream_t)stream);
+    if (e != cudaSuccess) return tc_fail(-2, cudaGetErrorString(e));
+  }
+  return 0;
+}
 
 int gbns_lg_prepare_tc(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
   if (!batch || !lg || batch->num_runs <= 0 || !lg->Phi_hi || !lg->Phi_lo || !lg->row_base || lg->total_rows < 1)

@@ -64,6 +64,7 @@ class RunSpec:
     N: int = 0
     log_L_offset: float = 0.0  # FP64 constant part of log L (device values are relative to it)
     gradient_guided: bool = False
+    gradient_slice: bool = False
 
 
 def ncoef_table(nmax: int) -> np.ndarray:
@@ -157,7 +158,8 @@ class NSBatch:
     """Device state of R independent runs."""
 
     def __init__(self, specs: List[RunSpec], device="cuda", chains_per_item: int = 64,
-                 max_evals_per_slice: int = 100000, wide_chains_per_item: int = 0, lg_tensor_cores: bool = True):
+                 max_evals_per_slice: int = 100000, wide_chains_per_item: int = 0, lg_tensor_cores: bool = True,
+                 chains_per_lane: int = 1, warp_min_D: int = 17, lg_fused: Optional[bool] = None):
         if not specs:
             raise ValueError("no runs")
         self.specs = specs
@@ -179,12 +181,13 @@ class NSBatch:
         self.lg = FAMILY_LINGAUSS in fams
         if self.lg and len(fams) > 1:
             raise ValueError("a batch holds either linear-Gaussian runs only or none")
-        gg = {bool(s.gradient_guided) for s in specs}
+        gg = {(bool(s.gradient_guided), bool(s.gradient_slice)) for s in specs}
         if len(gg) > 1:
-            raise ValueError("a batch holds either gradient-guided runs only or none")
-        self.gradient_guided = gg.pop()
-        if self.gradient_guided and any(s.family == FAMILY_LINGAUSS for s in specs):
-            raise NotImplementedError("the gradient-guided slice is not on the linear-Gaussian lock step")
+            raise ValueError("the runs of a batch share the slice sampler's gradient options")
+        self.gradient_guided, self.gradient_slice = gg.pop()
+        if (self.gradient_guided or self.gradient_slice) and any(s.family == FAMILY_LINGAUSS for s in specs):
+            raise NotImplementedError("the gradient options of the slice sampler are not on the linear-Gaussian "
+                                      "lock step")
         for r, s in enumerate(specs):
             validate_spec(s, r)
         live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])
@@ -200,7 +203,7 @@ class NSBatch:
         liveU_off, newU_off = excl(ns * Ws), excl(ss * Ws)
         phU_off, phL_off = excl(ss * Ks * Ws), excl(ss * Ks)
         self.offsets = dict(live=live_off, store=store_off, shell=shell_off, ustore=ustore_off, liveU=liveU_off,
-                            newU=newU_off, param=param_off)
+                            newU=newU_off, param=param_off, phU=phU_off, phL=phL_off)
 
         descs = (_ffi.RunDesc * R)()
         for r, s in enumerate(specs):
@@ -264,15 +267,26 @@ class NSBatch:
         # work items: (run, first chain, chain count), grouped by (family, D bucket),
         # longest (largest D) first inside a bucket
         CH = int(chains_per_item)
+        if int(chains_per_lane) < 1:
+            raise ValueError("chains_per_lane must be at least 1")
+        self.chains_per_lane = int(chains_per_lane)
         items = []
+        if not 2 <= int(warp_min_D) <= 17:
+            raise ValueError("warp_min_D must be in [2, 17]")
+        self.warp_min_D = int(warp_min_D)
         for r, s in enumerate(specs):
             if s.family == FAMILY_LINGAUSS:
                 continue
             b = s.family * 4 + _dbucket(s.D)
-            # warp-cooperative buckets (MVN, D > 16): one chain per lane of the CTA (256 lanes
-            # for D > 32, 512 for 16 < D <= 32), so the lanes of a CTA finish together
-            if s.family != FAMILY_MVN or s.D <= 16:
-                ch = CH
+            warp = s.family == FAMILY_MVN and s.D >= self.warp_min_D
+            if warp and b < 2:
+                b = 2  # a correlated Gaussian with D <= 16 on the warp-cooperative kernel (DMAX 32)
+            # warp-cooperative buckets: one chain per lane of the CTA (256 lanes for D > 32,
+            # 512 for D <= 32), each warp refilling its lanes from the CTA's pool
+            if not warp:
+                # one thread per chain, each CTA (CH lanes) drawing from a pool of
+                # CH * chains_per_lane chains
+                ch = CH * int(chains_per_lane)
             else:
                 ch = int(wide_chains_per_item) if wide_chains_per_item else (256 if s.D > 32 else 512)
             for c0 in range(0, s.shell_size, ch):
@@ -306,6 +320,7 @@ class NSBatch:
         b.chains_per_item = CH
         b.max_evals_per_slice = int(max_evals_per_slice)
         b.gradient_guided = int(self.gradient_guided)
+        b.gradient_slice = int(self.gradient_slice)
         self._b = b
         self._lgb = self._alloc_lg(specs, ss, Ds, shell_off, lg_tensor_cores) if self.lg else None
         self._graphs: Dict[tuple, tuple] = {}
@@ -317,6 +332,23 @@ class NSBatch:
         self.iterations_run = 0
         self.kernel_launches = 0
         self._kernels_per_iter = 1 + int(np.count_nonzero(be > bb))
+        # linear-Gaussian shells: one fused launch per shell when every run's share of Phi fits in
+        # the shared memory of its cluster (lg_fused=None: whenever it fits)
+        self.lg_fused = False
+        if self.lg and self.lg_tc and lg_fused is not False:
+            for cs in (16, 8):
+                plan = fused_plan([s.N for s in specs], int(self._lgb.pmax), (cs,))
+                if plan is not None:
+                    self._setup_fused(plan, ss)
+                    held = ctypes.c_int(0)
+                    _ffi.call("gbns_lg_fused_max_clusters", ctypes.byref(self._b), ctypes.byref(self._lgb),
+                              ctypes.byref(held))
+                    if held.value > 0:
+                        break
+                    self._teardown_fused()
+            if lg_fused and not self.lg_fused:
+                raise ValueError("the fused linear-Gaussian shell needs every run's rows per CTA x ceil(P / 32) "
+                                 "<= 512 with clusters of 8 or 16 CTAs that the device can hold")
 
     def _alloc_lg(self, specs, ss, Ds, shell_off, tensor_cores=True):
         """Lock-step chain state of the linear-Gaussian family + residual work items:
@@ -376,6 +408,24 @@ class NSBatch:
         self.lg_steps_run = 0
         return g
 
+    def _teardown_fused(self):
+        g = self._lgb
+        g.items_fused, g.num_items_fused, g.cluster_size, g.rows_per_cta = None, 0, 0, 0
+        self.lg_fused = False
+        self._kernels_per_iter = 1
+
+    def _setup_fused(self, plan, ss):
+        cs, rows = plan
+        items = [(r, c0) for r, s in enumerate(self.specs) for c0 in range(0, int(ss[r]), 128)]
+        self.lg_fused_t = torch.tensor(np.array(items, np.int32).reshape(-1, 2), device=self.device)
+        g = self._lgb
+        g.items_fused, g.num_items_fused = self.lg_fused_t.data_ptr(), len(items)
+        g.cluster_size, g.rows_per_cta = int(cs), int(rows)
+        g.max_steps = int(max(s.num_slices for s in self.specs)) * 2000
+        self.lg_fused = True
+        self._kernels_per_iter = 2  # fused shell + merge
+        self.fused_plan = {"cluster_size": int(cs), "rows_per_cta": int(rows), "clusters": len(items)}
+
     # ----------------------------------------------------------------- driving
     def _stream(self):
         """The current CUDA stream of the batch's device; a batch built on the CPU (layout only)
@@ -390,6 +440,11 @@ class NSBatch:
         self.kernel_launches += 2
 
     def iterate(self, k: int):
+        if self.lg and self.lg_fused:
+            _ffi.call("gbns_lg_iterate", ctypes.byref(self._b), ctypes.byref(self._lgb), int(k), self._stream())
+            self.iterations_run += k
+            self.kernel_launches += 2 * k
+            return
         if self.lg:
             for _ in range(k):
                 self._lg_iteration(use_graph=False)
@@ -429,7 +484,16 @@ class NSBatch:
 
     def _lg_iteration(self, use_graph: bool = True, block: int = 64):
         """One NS iteration of the linear-Gaussian batch: start the shell, advance every chain
-        in blocks of `block` likelihood evaluations until all chains are done, then merge."""
+        in blocks of `block` likelihood evaluations until all chains are done, then merge (with
+        the fused shell: one launch for the shell, then the merge)."""
+        if self.lg_fused:
+            if use_graph:
+                self.iterate_graph(1)
+            else:
+                _ffi.call("gbns_lg_iterate", ctypes.byref(self._b), ctypes.byref(self._lgb), 1, self._stream())
+                self.iterations_run += 1
+                self.kernel_launches += 2
+            return
         st = self.state()
         active = (st["done"] == 0) & (st["phase"] == 1)
         if not np.any(active):
@@ -480,9 +544,15 @@ class NSBatch:
                 if self.timing:
                     for a, b_ in evs:
                         _ffi.call("gbns_record_event", ctypes.c_void_p(a.cuda_event), self._stream())
-                        _ffi.call("gbns_batch_shell", ctypes.byref(self._b), self._stream())
+                        if self.lg_fused:
+                            _ffi.call("gbns_lg_shell_fused", ctypes.byref(self._b), ctypes.byref(self._lgb),
+                                      self._stream())
+                        else:
+                            _ffi.call("gbns_batch_shell", ctypes.byref(self._b), self._stream())
                         _ffi.call("gbns_record_event", ctypes.c_void_p(b_.cuda_event), self._stream())
                         _ffi.call("gbns_batch_merge", ctypes.byref(self._b), self._stream())
+                elif self.lg_fused:
+                    _ffi.call("gbns_lg_iterate", ctypes.byref(self._b), ctypes.byref(self._lgb), int(k), self._stream())
                 else:
                     _ffi.call("gbns_batch_iterate", ctypes.byref(self._b), int(k), self._stream())
             torch.cuda.current_stream().wait_stream(side)
@@ -500,6 +570,7 @@ class NSBatch:
     def _collect_timing(self):
         evs = getattr(self, "_pending_events", None)
         if evs:
+            evs[-1][1].synchronize()  # the graph's last event: every pair before it has completed
             self.shell_ms += sum(a.elapsed_time(b_) for a, b_ in evs)
             self.shell_launch_groups += len(evs)
         self._pending_events = None
@@ -544,7 +615,7 @@ class NSBatch:
             self._collect_timing()
             if done:
                 break
-            if self.lg:
+            if self.lg and not self.lg_fused:
                 self._lg_iteration(use_graph=use_graph)
                 done_it += 1
                 continue
@@ -686,6 +757,19 @@ class NSBatch:
         words = torch.from_numpy(np.ascontiguousarray(np.asarray(U, dt).ravel()).view(np.float32))
         self.live_U[p][uo:uo + n * int(self.ucols[r])].copy_(words)
         self.live_L[p][o:o + n].copy_(torch.from_numpy(np.asarray(log_L, np.float32)))
+
+
+def fused_plan(Ns, pmax: int, sizes=(16, 8)):
+    """(cluster size, rows per CTA) of the fused linear-Gaussian shell, or None when a run's
+    share of Phi would not fit: clusters of 16 (else 8) CTAs, each holding rows_per_cta rows
+    (128, 256 or 512) of TF32 hi / lo Phi, with rows_per_cta * ceil(pmax / 32) <= 512."""
+    nkb = 2 if pmax > 32 else 1
+    for cs in sizes:
+        need = max(128 * -(-int(N) // (cs * 128)) for N in Ns)
+        rows = next((r for r in (128, 256, 512) if r >= need), None)
+        if rows is not None and rows * nkb <= 512:
+            return cs, rows
+    return None
 
 
 # --------------------------------------------------------------- model tables

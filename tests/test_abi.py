@@ -123,41 +123,32 @@ def test_size_limits(lib):
     assert b"262143" in lib.gbns_last_error()
 
 
-def _doc_stub():
-    doc = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    block = doc.split("A complete ctypes binding", 1)[1].split("```python", 1)[1].split("```", 1)[0]
-    return block
-
-
-def test_integration_ctypes_stub_matches_header():
-    """The ctypes binding in INTEGRATION.md names every declared symbol with the header's
-    argument kinds (pointer / int / long long / double)."""
-    block = _doc_stub()
-    stub = {n: [a.strip() for a in args.replace("\n", " ").split(",") if a.strip()]
-            for n, args in re.findall(r"lib\.(gbns_\w+)\.argtypes = \[([^\]]*)\]", block)}
+def test_binding_matches_header():
+    """jaxns_gb300.binding declares every symbol of the header with the header's argument
+    kinds (pointer / int / long long / double)."""
+    from jaxns_gb300.binding import ARGTYPES
     protos = dict(_prototypes(), gbns_last_error=[])
-    assert set(stub) == set(protos) == set(_declared())
+    assert set(ARGTYPES) == set(protos) == set(_declared())
 
     def kind(t):
         if "*" in t:
-            return "P"
-        return {"double": "c_double", "long long": "c_longlong", "int": "c_int"}[t.replace("const ", "").strip()]
+            return ctypes.c_void_p
+        return {"double": ctypes.c_double, "long long": ctypes.c_longlong,
+                "int": ctypes.c_int}[t.replace("const ", "").strip()]
 
     for name, types in protos.items():
-        assert stub[name] == [kind(t) for t in types], name
+        assert ARGTYPES[name] == [kind(t) for t in types], name
 
 
-def test_integration_ctypes_stub_runs(lib):
-    """The documented stub binds the built library and its error paths answer through it."""
-    ns = {}
-    exec(_doc_stub().replace('ctypes.CDLL("jaxns_gb300/_lib/libgbns.so")', "LIB"),
-         {"LIB": ctypes.CDLL(lib._name)}, ns)
-    stub_lib = ns["lib"]
-    assert stub_lib.gbns_version() == 1
-    assert stub_lib.gbns_batch_iterate(None, 1, None) == -1
-    assert b"NULL" in stub_lib.gbns_last_error()
-    assert stub_lib.gbns_evidence_adjoint_tc(None, None, 0, 0, None, None, 0, 0.0, 0.0, None, None, None, None,
-                                             None, None, None) == -1
+def test_binding_runs(lib):
+    """The binding loads the built library and its error paths answer through it."""
+    from jaxns_gb300.binding import bind
+    b = bind(lib._name)
+    assert b.gbns_version() == 1
+    assert b.gbns_batch_iterate(None, 1, None) == -1
+    assert b"NULL" in b.gbns_last_error()
+    assert b.gbns_evidence_adjoint_tc(None, None, 0, 0, None, None, 0, 0.0, 0.0, None, None, None, None,
+                                      None, None, None) == -1
 
 
 def test_header_and_library_from_plain_c(lib, tmp_path):

@@ -27,19 +27,24 @@ def _specs():
 def test_items_cover_every_chain_once_and_buckets_are_contiguous():
     from jaxns_gb300.engine import NSBatch, _dbucket
     specs = _specs()
-    for cpi, wide in ((32, 0), (64, 256), (128, 512)):
-        b = NSBatch(specs, device="cpu", chains_per_item=cpi, wide_chains_per_item=wide)
+    for cpi, cpl, wide, wmin in ((32, 1, 0, 17), (64, 2, 256, 17), (128, 4, 512, 17), (64, 3, 0, 9)):
+        b = NSBatch(specs, device="cpu", chains_per_item=cpi, wide_chains_per_item=wide, chains_per_lane=cpl,
+                    warp_min_D=wmin)
         items = b.items.numpy()[: b._b.num_items]
         covered = [np.zeros(s.shell_size, np.int32) for s in specs]
         for r, c0, cnt, _ in items:
             covered[r][c0:c0 + cnt] += 1
-            wide_run = specs[r].family == 0 and specs[r].D > 16
-            assert cnt <= (wide or (256 if specs[r].D > 32 else 512)) if wide_run else cnt <= cpi
+            wide_run = specs[r].family == 0 and specs[r].D >= wmin
+            # thread-per-chain CTAs draw from a pool of cpi * cpl chains
+            assert cnt <= (wide or (256 if specs[r].D > 32 else 512)) if wide_run else cnt <= cpi * cpl
         assert all(np.all(c == 1) for c in covered)
         for k in range(8):
             lo, hi = b._b.bucket_begin[k], b._b.bucket_end[k]
             for r, *_ in items[lo:hi]:
-                assert specs[r].family * 4 + _dbucket(specs[r].D) == k
+                expect = specs[r].family * 4 + _dbucket(specs[r].D)
+                if specs[r].family == 0 and specs[r].D >= wmin:
+                    expect = max(expect, 2)  # correlated Gaussians on the warp-cooperative kernel
+                assert expect == k
             Ds = [specs[r].D for r, *_ in items[lo:hi]]
             assert Ds == sorted(Ds, reverse=True)     # longest (largest D) first in a bucket
         assert sum(b._b.bucket_end[k] - b._b.bucket_begin[k] for k in range(8)) == len(items)
