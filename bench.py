@@ -79,6 +79,15 @@ def workload(R: int, seed: int = 2024, name: str = "shells"):
         for r in range(R):
             out.append((SHELLS_D, "shells", (c1, -c1, 2.0, 0.1), 1000, 50, 100000))
         return out
+    if name == "gh168":
+        # the reference's published benchmark problem (benchmarks/gh168/main.py): D = 8, prior
+        # MultivariateNormalTriL(15, I), likelihood N(0, Sigma) with 0.99 correlations; jaxns's
+        # defaults: 30 D live points, 5 D slices, max_samples 1e5
+        D = 8
+        data_cov = np.where(np.eye(D) == 1, 1.0, 0.99)
+        for r in range(R):
+            out.append((D, "gh168", (15.0 * np.ones(D), np.eye(D), np.zeros(D), data_cov), 30 * D, 5 * D, 100000))
+        return out
     rng = np.random.default_rng(seed)
     Ds = rng.integers(2, 65, size=R)
     for r, D in enumerate(Ds):
@@ -103,11 +112,27 @@ def shells_log_Z(D=SHELLS_D, R=2.0, w=0.1, box=12.0):
     return np.log(2 * S * I) - D * np.log(box)
 
 
+def gh168_log_Z(prior_mu, prior_L, data_mu, data_cov):
+    S = prior_L @ prior_L.T + data_cov
+    d = data_mu - prior_mu
+    return float(-0.5 * d @ np.linalg.solve(S, d) - 0.5 * np.linalg.slogdet(2 * np.pi * S)[1])
+
+
 def make_samplers(wl):
     import jaxns_gb300 as gb
     samplers = []
     cache = {}
     for D, kind, params, n, S, cap in wl:
+        if kind == "gh168":
+            if "gh168" not in cache:
+                pm, pL, dm, dc = params
+
+                def prior_model(pm=pm, pL=pL):
+                    x = yield gb.Prior(gb.MultivariateNormalTriL(pm, pL), name="x")
+                    return x
+                cache["gh168"] = gb.Model(prior_model, gb.MultivariateNormalLikelihood(dm, dc))
+            samplers.append(gb.NestedSampler(cache["gh168"], max_samples=cap, store_U=False))
+            continue
         if kind == "shells":
             if "shells" not in cache:
                 def prior_model(D=D):
@@ -129,7 +154,9 @@ def oracle_models(wl, idx):
     models, cfgs = [], []
     for r in idx:
         D, kind, params, n, S, cap = wl[r]
-        if kind == "shells":
+        if kind == "gh168":
+            models.append(oracle.mvn_tril_prior_model(params[0], params[1], params[2], params[3]))
+        elif kind == "shells":
             models.append(oracle.shells_model(-6, 6, params[0], params[1], params[2], params[3]))
         else:
             models.append(oracle.mvn_model(-10 * np.ones(D), 10 * np.ones(D), params[0], params[1]))
@@ -189,7 +216,8 @@ def cpu_sample(wl, idx, iters: int, threads: int):
     models, cfgs = oracle_models(wl, idx)
     keys = np.array([oracle.PRNGKey(r) for r in idx])
     tcs = [{"dlogZ": 1e-4}] * len(idx)
-    return oracle.ns_run_batch_timed(models, cfgs, keys, tcs, threads, iters)
+    log_Z, nev, _, secs, its = oracle.ns_run_batch(models, cfgs, keys, tcs, threads, iters, timed=True)
+    return secs, nev, its, log_Z
 
 
 def iterations_model(D: int) -> float:
@@ -201,15 +229,15 @@ def cpu_runs_per_s(wl, name, threads):
     """Host runs/s of the oracle on this workload.  shells: `threads` complete runs on
     `threads` host threads.  config3: every (R/16)-th run for 2 NS iterations, scaled to whole
     runs by the expected iteration count."""
-    if name == "shells":
+    if name in ("shells", "gh168"):
         idx = list(range(min(threads, len(wl))))
-        secs, evals, its = cpu_sample(wl, idx, 0, threads)
+        secs, evals, its, log_Z = cpu_sample(wl, idx, 0, threads)
         t = float(np.max(secs))  # the threads ran concurrently
-        return len(idx) / t, dict(runs=len(idx), seconds=float(np.sum(secs)),
+        return len(idx) / t, dict(runs=len(idx), seconds=float(np.sum(secs)), log_Z=log_Z, idx=idx,
                                   sample=f"{len(idx)} complete runs on {threads} host threads")
     stride = max(1, len(wl) // 16)
     idx = list(range(0, len(wl), stride))
-    secs, evals, its = cpu_sample(wl, idx, 2, threads)
+    secs, evals, its, _ = cpu_sample(wl, idx, 2, threads)
     t_est = sum(secs[k] / max(its[k], 1) * max(iterations_model(wl[r][0]), its[k]) for k, r in enumerate(idx))
     t_total = t_est * stride
     return len(wl) / (t_total / threads), dict(
@@ -222,9 +250,10 @@ def cpu_runs_per_s(wl, name, threads):
 
 def flops_per_eval(D, kind):
     """Algorithmic FP32 flops of one likelihood evaluation: MVN D^2 + 8D (proposal, prior
-    quantile, triangular solve, sum of squares); shells 10D + 22 (proposal, quantile, two
-    norms, shell terms, logaddexp)."""
-    return D * D + 8 * D if kind == "mvn" else 10 * D + 22
+    quantile, triangular solve, sum of squares; the TriL prior's matvec is folded into the
+    likelihood's factor); shells 10D + 22 (proposal, quantile, two norms, shell terms,
+    logaddexp)."""
+    return D * D + 8 * D if kind in ("mvn", "gh168") else 10 * D + 22
 
 
 def main():
@@ -233,7 +262,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gbns", choices=["gbns", "reference"])
-    ap.add_argument("--workload", default="shells", choices=["shells", "config3", "blr", "blr_batch"])
+    ap.add_argument("--workload", default="shells", choices=["shells", "config3", "blr", "blr_batch", "gh168"])
     ap.add_argument("--runs", type=int, default=None)
     ap.add_argument("--block", type=int, default=16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -253,11 +282,19 @@ def main():
                     help="blr workloads: fp32 CUDA-core residuals instead of the tcgen05 kernel")
     ap.add_argument("--iterations", type=int, default=None,
                     help="time init + this many NS iterations instead of whole runs (kernel profiling)")
+    ap.add_argument("--chains-per-lane", type=int, default=1,
+                    help="chain pool of each thread-per-chain sampler CTA, in chains per lane")
+    ap.add_argument("--chains-per-item", type=int, default=64, help="CTA width of the thread-per-chain sampler")
+    ap.add_argument("--warp-min-d", type=int, default=17,
+                    help="correlated Gaussians with D >= this run on the warp-cooperative sampler")
+    ap.add_argument("--no-adjoint", action="store_true",
+                    help="shells workload: skip the adjoint sub-record (configs[3]: one linear-regression "
+                         "problem, fused forward + adjoint against the plain GPU path + finite differences)")
     args = ap.parse_args()
     if args.workload in ("blr", "blr_batch"):
         return main_blr(args)
     if args.runs is None:
-        args.runs = 1024 if args.workload == "shells" else 4096
+        args.runs = 1024 if args.workload in ("shells", "gh168") else 4096
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -271,6 +308,10 @@ def main():
     if args.workload == "shells":
         wdesc = (f"Gaussian shells D=10 (R=2, w=0.1, centres +-3.5 e0, U[-6,6]^10), 1000 live points, "
                  f"50 slices, dlogZ<1e-4; {args.runs} independent seeds per GPU in one batched launch")
+    elif args.workload == "gh168":
+        wdesc = (f"reference benchmark gh168: D=8, prior MultivariateNormalTriL(15, I), likelihood N(0, Sigma) "
+                 f"with 0.99 correlations, NestedSampler defaults (240 live points, 40 slices, max_samples 1e5, "
+                 f"default termination); {args.runs} independent seeds per GPU in one batched launch")
     else:
         wdesc = (f"batched correlated Gaussians: {args.runs} runs per GPU, D~U{{2..64}}, n=50D, S=5D, "
                  f"dlogZ<1e-4")
@@ -309,8 +350,10 @@ def main():
     samplers = make_samplers(wl)
     keys = replica_keys(rank, len(wl))  # independent seeds on every rank
     tune = args.autotune or (args.workload == "config3" and not args.no_autotune)
-    bns = BatchedNestedSampler(samplers, keys, [gb.TerminationCondition(dlogZ=1e-4)] * len(wl), block=args.block,
-                               autotune=tune)
+    tcs = [None if args.workload == "gh168" else gb.TerminationCondition(dlogZ=1e-4)] * len(wl)
+    bns = BatchedNestedSampler(samplers, keys, tcs, block=args.block,
+                               autotune=tune, chains_per_item=args.chains_per_item,
+                               chains_per_lane=args.chains_per_lane, warp_min_D=args.warp_min_d)
     b = bns.batch
     if args.iterations is not None:
         # kernel-profiling mode: init + a fixed number of eager iterations, no results pass
@@ -376,16 +419,35 @@ def main():
     shell_s = b.shell_ms / 1e3
     clocks = clk.summary()
     sm_mhz = clocks["sm_mhz"] or 1900.0
-    fp32_peak = 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+    sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+    fp32_peak = sms * 128 * 2 * sm_mhz * 1e6 / 1e12
     achieved = flops / shell_s / 1e12 if shell_s > 0 else None
     roofline = {"bound": "fp32", "kernel": "k_slice_shell (fused slice sampler)", "achieved": achieved,
                 "peak": fp32_peak, "unit": "TFLOP/s", "frac": (achieved / fp32_peak) if achieved else None,
                 "traffic": None,
-                "peak_source": "derived: 152 SMs x 128 FP32 lanes x 2 flop x median SM clock under load "
+                "peak_source": f"derived: {sms} SMs x 128 FP32 lanes x 2 flop x median SM clock under load "
                                "(MEASURED_PEAKS.json has no FP32 CUDA-core figure)",
                 "flops_per_eval": "MVN D^2+8D, shells 10D+22",
                 "sampler_share_of_step": shell_s / (ms / 1e3) if ms else None,
                 "sampler_launch_groups": b.shell_launch_groups}
+    # the resource that binds the sampler: instruction issue.  Its algorithmic instruction
+    # stream is the threefry-2x32 blocks that reproduce jax.random (72 integer operations each:
+    # 20 rounds of add, rotate, xor and 6 key injections of two adds) plus the likelihood flops;
+    # per chain 6 key blocks, 5 per slice start, 3 per shrink step and D per direction (S
+    # directions), so blocks = chains (6 + 2 S + S D) + 3 evaluations.  Achieved = those
+    # operations / 32 lanes / sampler time, against 4 warp instructions per SM per clock.
+    its = st["iterations"].astype(np.float64)
+    Ss = np.array([w[4] for w in wl], np.float64)
+    chains = its * np.array([w[3] // 2 for w in wl], np.float64)
+    blocks = chains * (6 + 2 * Ss + Ss * Dr) + 3.0 * st["num_likelihood_evaluations"].astype(np.float64)
+    int_ops = float(np.sum(blocks)) * 72.0 * args.steps
+    issue_peak = 4.0 * sms * sm_mhz * 1e6 / 1e12  # tera warp-instructions per second
+    issue_achieved = (int_ops + flops) / 32.0 / shell_s / 1e12 if shell_s > 0 else None
+    roofline_issue = {"bound": "issue", "kernel": "k_slice_shell (fused slice sampler)", "achieved": issue_achieved,
+                      "peak": issue_peak, "unit": "T warp-instructions/s",
+                      "frac": issue_achieved / issue_peak if issue_achieved else None,
+                      "counted": "threefry integer ops (72 per block) + likelihood flops, at full SIMT width",
+                      "threefry_blocks_per_eval": float(np.sum(blocks) / max(1.0, float(np.sum(st["num_likelihood_evaluations"]))))}
 
     # ---- end-to-end through the public API: run table + keys from pinned host memory, the
     # [R, 8] summary (log Z, uncertainty, ESS, H, counts) back to the host
@@ -402,23 +464,37 @@ def main():
     e2e = {"value": runs_total / (e2e_ms / 1e3), "unit": "runs/s", "h2d_bytes_per_step": h2d,
            "d2h_bytes_per_step": d2h}
 
-    truth = np.full(len(wl), shells_log_Z()) if args.workload == "shells" else -Dr * np.log(20.0)
+    if args.workload == "shells":
+        truth = np.full(len(wl), shells_log_Z())
+    elif args.workload == "gh168":
+        truth = np.full(len(wl), gh168_log_Z(*wl[0][2]))
+    else:
+        truth = -Dr * np.log(20.0)
     dz = sc[:, 0] - truth
-    accuracy = {"truth": "FP64 radial quadrature" if args.workload == "shells" else "analytic -D log 20",
+    accuracy = {"truth": {"shells": "FP64 radial quadrature", "gh168": "analytic log N(0; 15, I + Sigma)"}.get(
+                    args.workload, "analytic -D log 20"),
                 "mean_log_Z": float(np.mean(sc[:, 0])), "truth_log_Z": float(np.mean(truth)),
                 "mean_abs_dlogZ": float(np.mean(np.abs(dz))), "frac_abs_dlogZ_lt_0.1": float(np.mean(np.abs(dz) < 0.1)),
                 "frac_within_3sigma": float(np.mean(np.abs(dz) < 3 * sc[:, 1])),
                 "mean_log_Z_uncert": float(np.mean(sc[:, 1])), "ensemble_mean_error": float(np.mean(dz))}
 
+    # the only published number for this path: 1.108 s per gh168 run (jaxns 2.6.2, JAX CPU,
+    # benchmarks/gh168/results), i.e. 0.903 runs/s
+    vs_baseline = value / (1.0 / 1.108) if args.workload == "gh168" else None
     line = {"metric": METRIC, "value": value, "unit": "runs/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32 (FP64 evidence)", "data": "synthetic (seeded)",
+            "vs_baseline": vs_baseline, "dtype": "f32 (FP64 evidence)", "data": "synthetic (seeded)",
             "config": {"workload": wdesc, "runs_per_gpu": args.runs, "graph_block": args.block,
                        "l2": "per-step sample store > L2 (no flush needed)",
-                       "launch_shape": ({k: bns.tuning[k] for k in ("chains_per_item", "wide_chains_per_item")}
-                                        if bns.tuning else {"chains_per_item": 64, "wide_chains_per_item": "default"}),
+                       "launch_shape": ({k: bns.tuning[k] for k in ("chains_per_item", "chains_per_lane",
+                                                                     "wide_chains_per_item", "warp_min_D")}
+                                        if bns.tuning else {"chains_per_item": args.chains_per_item,
+                                                            "chains_per_lane": args.chains_per_lane,
+                                                            "wide_chains_per_item": "default",
+                                                            "warp_min_D": args.warp_min_d}),
                        "autotune_table": bns.tuning["table"] if bns.tuning else None},
             "likelihood_evals_per_s": evals_per_s, "gpu_launches": int(gpu_launches), "roofline": roofline,
+            "roofline_issue": roofline_issue,
             "e2e": e2e, "clocks": clocks, "accuracy": accuracy,
             "iterations": {"max": int(st["iterations"].max()), "mean": float(st["iterations"].mean())}}
 
@@ -439,12 +515,25 @@ def main():
         plain = len(idx) / tot
         line["plain_single_run_loop"] = {"runs_per_s": plain, "sample": f"{len(idx)} runs one at a time, eager launches",
                                          "batched_speedup": value / world / plain}
+    if rank == 0 and args.workload == "shells" and not args.no_adjoint:
+        line["adjoint"] = adjoint_record()
     if rank == 0 and not args.no_cpu:
         from oracle import oracle
         oracle.build()
         v, info = cpu_runs_per_s(wl, args.workload, threads)
         line["cpu_baseline"] = {"value": v, "unit": "runs/s", "cores": threads, "kind": "port",
                                 "sample": info["sample"]}
+        if "log_Z" in info:
+            # accuracy of the CPU arm on the same seeds (PRNGKey(0..k-1)) next to the GPU's
+            k = len(info["idx"])
+            dzr = np.asarray(info["log_Z"]) - truth[:k]
+            dzg = sc[:k, 0] - truth[:k]
+            line["reference_accuracy"] = {
+                "runs": k, "seeds": f"PRNGKey(0..{k - 1})",
+                "oracle_frac_abs_dlogZ_lt_0.1": float(np.mean(np.abs(dzr) < 0.1)),
+                "oracle_mean_error": float(np.mean(dzr)), "oracle_mean_abs_dlogZ": float(np.mean(np.abs(dzr))),
+                "gpu_frac_abs_dlogZ_lt_0.1": float(np.mean(np.abs(dzg) < 0.1)),
+                "gpu_mean_error": float(np.mean(dzg)), "gpu_mean_abs_dlogZ": float(np.mean(np.abs(dzg)))}
     if rank == 0:
         print(json.dumps(check_line(line, e2e=True, cpu=not args.no_cpu)))
     if world > 1:
@@ -530,6 +619,71 @@ def blr_gradient_se(b, res, wl, thetas):
         var = (pw[:, None] * (g - mean) ** 2).sum(0)
         se[r] = torch.sqrt(var * (pw * pw).sum()).cpu().numpy()
     return se
+
+
+def adjoint_record(h: float = 1e-3) -> dict:
+    """The metric's adjoint half on configs[3] (Bayesian linear regression, Phi 4096 x 32, 1024
+    live points): one problem's NS run + reweighted-evidence adjoint (log Z and
+    d log Z / d(log tau, log sigma)) through the batched engine and a captured graph, timed with
+    CUDA events after one warm-up, against the plain GPU path (eager launches, no graph) plus
+    central finite differences (five runs: theta, log tau +- h, log sigma +- h); errors against
+    the analytic evidence and gradient."""
+    import torch
+    import jaxns_gb300 as gb
+    from jaxns_gb300.adjoint import batch_evidence_and_grad, blr_log_evidence
+    from jaxns_gb300.batched import BatchedNestedSampler
+    from jaxns_gb300.engine import NSBatch
+    p = blr_workload(1, 2024, "blr")[0]
+    key = np.asarray(gb.random.PRNGKey(0), np.uint32).reshape(1, 2)
+    bns = BatchedNestedSampler([blr_sampler(p)], key, None, store_U=True)
+    b = bns.batch
+    thetas = np.array([[np.log(p["tau"]), np.log(p["sigma"])]])
+
+    def fused():
+        bns(from_host=False)
+        res = b.results(with_U=True)
+        return res, batch_evidence_and_grad(b, res, thetas)
+
+    fused()  # warm-up: graphs, kernels, buffers
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    res, adj = fused()
+    e1.record()
+    torch.cuda.synchronize()
+    fused_s = e0.elapsed_time(e1) / 1e3
+    lz = float(res["scalars"][0, 0].item())
+    lz_unc = float(res["scalars"][0, 1].item())
+    g = adj[0, 1:3].cpu().numpy()
+    se = blr_gradient_se(b, res, [p], thetas)[0]
+    lz_true, g_true = blr_log_evidence(p["Phi"].astype(np.float64), p["y"].astype(np.float64), thetas[0, 0],
+                                       thetas[0, 1])
+    g_true = np.asarray(g_true)
+    # plain GPU path + finite differences
+    t_plain, lzs = 0.0, []
+    for dlt, dls in [(0, 0), (h, 0), (-h, 0), (0, h), (0, -h)]:
+        ns = blr_sampler(p, dlt, dls)
+        one = NSBatch([ns.nested_sampler.run_spec(key[0], ns.normalise_term_cond(None))], lg_fused=False)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        one.run(use_graph=False)
+        sc = one.results(with_U=False)["scalars"].cpu().numpy()
+        t_plain += time.time() - t0
+        lzs.append(float(sc[0, 0]))
+        del one
+    fd = np.array([(lzs[1] - lzs[2]) / (2 * h), (lzs[3] - lzs[4]) / (2 * h)])
+    return {"workload": "Bayesian linear regression, Phi 4096x32 ~ N(0,1), sigma=0.5, tau=1, 1024 live points, "
+                        "num_slices=5P; one problem, NS run + reweighted-evidence adjoint",
+            "fused_s": fused_s, "plain_gpu_plus_fd_s": t_plain, "fused_speedup": t_plain / fused_s,
+            "plain": "five eager single-problem runs (theta, log tau +- 1e-3, log sigma +- 1e-3) on the two-launch "
+                     "lock step (chain step + tcgen05 residual per likelihood evaluation, no graph), central "
+                     "differences",
+            "fused_path": "k_lg_shell_fused" if b.lg_fused else "two-launch lock step",
+            "dlogZ": lz - float(lz_true), "log_Z_uncert": lz_unc,
+            "grad": [float(v) for v in g], "grad_analytic": [float(v) for v in g_true],
+            "grad_rel_err": [float(v) for v in np.abs(g - g_true) / np.abs(g_true)],
+            "grad_err_over_mc_se": [float(v) for v in np.abs(g - g_true) / se],
+            "fd_grad_rel_err": [float(v) for v in np.abs(fd - g_true) / np.abs(g_true)]}
 
 
 def main_blr(args):
@@ -658,30 +812,38 @@ def main_blr(args):
     T = args.iterations or 6
     b.timing = True
     b.resid_ms, b.resid_launches = 0.0, 0
+    b.shell_ms, b.shell_launch_groups = 0.0, 0
     b.reset()
     b.init()
     e0 = b.state()["num_likelihood_evaluations"].astype(np.float64)
     for _ in range(T):
         b._lg_iteration(use_graph=True)
+        b._collect_timing()
     e1 = b.state()["num_likelihood_evaluations"].astype(np.float64)
     b.timing = False
     rflops = float(np.sum((e1 - e0) * Ns * Ps * 2.0))
-    achieved = rflops / (b.resid_ms / 1e3) / 1e12 if b.resid_ms > 0 else None
+    # fused shells: events around every fused launch (chain logic, MMAs and cluster exchange
+    # together); two-launch lock step: events around every residual launch
+    kernel_ms = b.shell_ms if b.lg_fused else b.resid_ms
+    achieved = rflops / (kernel_ms / 1e3) / 1e12 if kernel_ms > 0 else None
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {"bf16_tflops": 1900.0}
     # the residual launches are timed inside seconds of continuous lock-step work: the sustained
     # (power-capped) dense bf16 figure is the denominator when the file has it
     peak_key = "bf16_tflops_sustained" if "bf16_tflops_sustained" in peaks else "bf16_tflops"
     peak = float(peaks[peak_key])
-    roofline = {"bound": "tensor", "kernel": "k_lg_resid_tc (3xTF32 tcgen05 Phi w residuals)", "achieved": achieved,
+    kname = ("k_lg_shell_fused (whole shell: chain steps + 3xTF32 tcgen05 Phi w residuals, clusters of "
+             f"{b.fused_plan['cluster_size']} CTAs, {b.fused_plan['rows_per_cta']} Phi rows per CTA)" if b.lg_fused
+             else "k_lg_resid_tc (3xTF32 tcgen05 Phi w residuals)")
+    roofline = {"bound": "tensor", "kernel": kname, "achieved": achieved,
                 "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak if achieved else None, "traffic": None,
                 "peak_source": f"MEASURED_PEAKS.json {peak_key} (dense bf16, of measured; the kernel runs inside a "
                                "long step); dense TF32 issues at half that rate and 3xTF32 issues three MMAs per "
                                "algorithmic product, so the ceiling of this formulation is peak/6",
                 "frac_of_3xtf32_ceiling": achieved / (peak / 6.0) if achieved else None,
                 "flops": "algorithmic 2 N P per likelihood evaluation (proposal x all data rows)",
-                "timed_iterations": T, "residual_launches": b.resid_launches,
-                "residual_ms": b.resid_ms}
+                "timed_iterations": T, "residual_launches": b.resid_launches or b.shell_launch_groups,
+                "kernel_ms": kernel_ms}
 
     # end-to-end: Phi, y, sigma and the run table from pinned host memory, per-problem
     # (log Z, uncertainty, log Z(theta), gradient) back to the host
@@ -726,7 +888,7 @@ def main_blr(args):
             lz = []
             for dlt, dls in [(0, 0), (h, 0), (-h, 0), (0, h), (0, -h)]:
                 ns = blr_sampler(wl[r], dlt, dls)
-                one = NSBatch([ns.nested_sampler.run_spec(keys[r], ns.normalise_term_cond(None))])
+                one = NSBatch([ns.nested_sampler.run_spec(keys[r], ns.normalise_term_cond(None))], lg_fused=False)
                 torch.cuda.synchronize()
                 t0 = time.time()
                 one.run(use_graph=False)

@@ -3,7 +3,7 @@
 Drop-in names: Model, Prior, NestedSampler / DefaultNestedSampler, TerminationCondition,
 NestedSamplerResults.  Compute runs in libgbns.so (hand-written CUDA); there is no CPU path.
 """
-from .framework import Model, Prior, Uniform, Normal, InvalidPriorName
+from .framework import Model, Prior, Uniform, Normal, MultivariateNormalTriL, InvalidPriorName
 from .likelihoods import MultivariateNormalLikelihood, GaussianShellsLikelihood, LinearGaussianLikelihood
 from .public import (TerminationCondition, NestedSamplerResults, NestedSampler, DefaultNestedSampler,
                      UniDimSliceSampler, UniformSampler, ShardedStaticNestedSampler, NestedSamplerState,

@@ -3,8 +3,9 @@
 
 A fused CUDA likelihood cannot be an arbitrary Python callable, so ``log_likelihood`` is
 one of the registered likelihood families of :mod:`jaxns_gb300.likelihoods`; priors are
-Uniform or Normal quantile transforms per U dimension (the quantiles jaxns applies through
-WrappedTFPDistribution._forward, framework/wrapped_tfp_distribution.py:77-84).
+Uniform or Normal quantile transforms per U dimension, or a MultivariateNormalTriL block (the
+standard normal quantile per dimension followed by the affine bijector loc + L z), as jaxns
+applies them through WrappedTFPDistribution._forward (framework/wrapped_tfp_distribution.py:77-84).
 """
 from __future__ import annotations
 
@@ -52,12 +53,35 @@ class Normal:
         return np.full(size, PRIOR_NORMAL, np.int32), a, b
 
 
+class MultivariateNormalTriL:
+    """MultivariateNormalTriL(loc, scale_tril): a D-dimensional Gaussian prior block.  Its U->X
+    map is the reference's: the base distribution's quantile per dimension (standard normal,
+    z = ndtri(u)) followed by the bijector X = loc + L z (tfp's MultivariateNormalTriL is a
+    transformed Sample(Normal(0, 1), D))."""
+
+    def __init__(self, loc, scale_tril):
+        self.loc = np.asarray(loc, np.float64).reshape(-1)
+        L = np.asarray(scale_tril, np.float64)
+        D = self.loc.shape[0]
+        if L.shape != (D, D):
+            raise ValueError(f"scale_tril must be [{D}, {D}], got {L.shape}")
+        if not np.all(np.diag(L) > 0):
+            raise ValueError("scale_tril must have a positive diagonal")
+        self.scale_tril = np.tril(L)
+        self.shape = (D,)
+
+    def table(self):
+        D = self.shape[0]
+        return np.full(D, PRIOR_NORMAL, np.int32), np.zeros(D), np.ones(D)
+
+
 class Prior:
     """A named prior over a block of U dimensions (framework/prior.py:65)."""
 
     def __init__(self, dist_or_value, name: Optional[str] = None):
-        if not isinstance(dist_or_value, (Uniform, Normal)):
-            raise ValueError("Prior supports Uniform and Normal distributions on the fused GPU path")
+        if not isinstance(dist_or_value, (Uniform, Normal, MultivariateNormalTriL)):
+            raise ValueError("Prior supports Uniform, Normal and MultivariateNormalTriL distributions on the fused "
+                             "GPU path")
         self.dist = dist_or_value
         self.name = name
 
@@ -87,6 +111,7 @@ class Model:
         self._params = params
         priors: List[_ParsedPrior] = []
         kinds, a_s, b_s = [], [], []
+        tril_blocks = []
         gen = prior_model()
         names = set()
         start = 0
@@ -101,6 +126,8 @@ class Model:
                 names.add(name)
                 k, a, b = p.dist.table()
                 priors.append(_ParsedPrior(name, p.dist.shape, start, p.size))
+                if isinstance(p.dist, MultivariateNormalTriL):
+                    tril_blocks.append((start, p.dist.loc, p.dist.scale_tril))
                 kinds.append(k)
                 a_s.append(a)
                 b_s.append(b)
@@ -109,6 +136,7 @@ class Model:
         except StopIteration:
             pass
         self.priors = priors
+        self.tril_blocks = tril_blocks  # (first dimension, loc, L) of every MultivariateNormalTriL block
         self.U_ndims = start
         self.prior_kind = np.concatenate(kinds) if kinds else np.zeros(0, np.int32)
         self.prior_a = np.concatenate(a_s) if a_s else np.zeros(0)
@@ -126,15 +154,28 @@ class Model:
         return {p.name: X[..., p.start:p.start + p.size].reshape(X.shape[:-1] + tuple(p.shape))
                 for p in self.priors if not p.name.startswith("__prior_")}
 
+    def _quantiles(self, Ut):
+        """Per-dimension quantile outputs q (X for Uniform / Normal dimensions, the standard
+        normal z of MultivariateNormalTriL dimensions) and X."""
+        import torch
+        a = torch.as_tensor(self.prior_a, dtype=Ut.dtype, device=Ut.device)
+        b = torch.as_tensor(self.prior_b, dtype=Ut.dtype, device=Ut.device)
+        normal = torch.as_tensor(self.prior_kind == PRIOR_NORMAL, device=Ut.device)
+        q = a + b * torch.where(normal, np.sqrt(2.0) * torch.erfinv(2.0 * Ut - 1.0), Ut)
+        X = q
+        if self.tril_blocks:
+            X = q.clone()
+            for s0, loc, L in self.tril_blocks:
+                D = len(loc)
+                Lt = torch.as_tensor(L, dtype=Ut.dtype, device=Ut.device)
+                X[..., s0:s0 + D] = torch.as_tensor(loc, dtype=Ut.dtype, device=Ut.device) + q[..., s0:s0 + D] @ Lt.T
+        return q, X
+
     def transform_flat(self, U):
         import torch
         is_t = isinstance(U, torch.Tensor)
         Ut = U if is_t else torch.as_tensor(np.asarray(U, np.float64))
-        a = torch.as_tensor(self.prior_a, dtype=Ut.dtype, device=Ut.device)
-        b = torch.as_tensor(self.prior_b, dtype=Ut.dtype, device=Ut.device)
-        normal = torch.as_tensor(self.prior_kind == PRIOR_NORMAL, device=Ut.device)
-        q = torch.where(normal, np.sqrt(2.0) * torch.erfinv(2.0 * Ut - 1.0), Ut)
-        X = a + b * q
+        X = self._quantiles(Ut)[1]
         return X if is_t else X.numpy()
 
     def log_prob_prior(self, U):
@@ -142,15 +183,33 @@ class Model:
         numpy array otherwise."""
         import torch
         is_t = isinstance(U, torch.Tensor)
-        X = self.transform_flat(U if is_t else torch.as_tensor(np.asarray(U, np.float64)))
+        Ut = U if is_t else torch.as_tensor(np.asarray(U, np.float64))
+        q, X = self._quantiles(Ut)
         a = torch.as_tensor(self.prior_a, dtype=X.dtype, device=X.device)
         b = torch.as_tensor(self.prior_b, dtype=X.dtype, device=X.device)
         normal = torch.as_tensor(self.prior_kind == PRIOR_NORMAL, device=X.device)
-        inside = (X >= a) & (X <= a + b)
-        lp_u = torch.where(inside, -torch.log(b), torch.full_like(X, -float("inf")))
-        lp_n = -0.5 * ((X - a) / b) ** 2 - torch.log(b) - 0.5 * np.log(2.0 * np.pi)
+        inside = (q >= a) & (q <= a + b)
+        lp_u = torch.where(inside, -torch.log(b), torch.full_like(q, -float("inf")))
+        lp_n = -0.5 * ((q - a) / b) ** 2 - torch.log(b) - 0.5 * np.log(2.0 * np.pi)
         lp = torch.where(normal, lp_n, lp_u).sum(-1)
+        # a MultivariateNormalTriL block: log N(X; loc, L L^T) = sum over its z of the standard
+        # normal density - sum log L_ii
+        for s0, loc, L in self.tril_blocks:
+            lp = lp - float(np.sum(np.log(np.diag(L))))
         return lp if is_t else lp.numpy()
+
+    def affine(self):
+        """(A, c) with X = A q + c over all dimensions (A lower triangular: identity except the
+        MultivariateNormalTriL blocks), or None when the model has no such block."""
+        if not self.tril_blocks:
+            return None
+        D = self.U_ndims
+        A, c = np.eye(D), np.zeros(D)
+        for s0, loc, L in self.tril_blocks:
+            k = len(loc)
+            A[s0:s0 + k, s0:s0 + k] = L
+            c[s0:s0 + k] = loc
+        return A, c
 
     @property
     def U_placeholder(self):

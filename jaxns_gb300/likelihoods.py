@@ -25,7 +25,19 @@ class MultivariateNormalLikelihood:
             raise ValueError(f"likelihood has dimension {len(self.mu)}, model has {D}")
 
     def params(self, model) -> np.ndarray:
-        return mvn_params(self.mu, self.cov)
+        aff = model.affine() if model is not None else None
+        if aff is None:
+            return mvn_params(self.mu, self.cov)
+        # a MultivariateNormalTriL prior X = A q + c folds into the likelihood's triangular
+        # factor: Linv (X - mu) = (Linv A) (q - A^-1 (mu - c)), so the kernels see a correlated
+        # Gaussian in q with mean A^-1 (mu - c) and factor Linv A (lower triangular)
+        A, c = aff
+        Linv = np.linalg.inv(self.L)
+        mu_q = np.linalg.solve(A, self.mu - c)
+        M = np.tril(Linv @ A)
+        D = len(self.mu)
+        c0 = -np.sum(np.log(np.diag(self.L))) - 0.5 * D * np.log(2.0 * np.pi)
+        return np.concatenate([mu_q, M.ravel(), [c0]]).astype(np.float32)
 
     def log_L_offset(self) -> float:
         return mvn_offset(self.cov)
@@ -51,6 +63,9 @@ class GaussianShellsLikelihood:
             raise ValueError("shell centres must have the model's dimension")
 
     def params(self, model) -> np.ndarray:
+        if model is not None and model.affine() is not None:
+            raise NotImplementedError("MultivariateNormalTriL priors are supported with the correlated-Gaussian "
+                                      "likelihood")
         return shells_params(self.c1, self.c2, self.radius, self.width)
 
     def log_L_offset(self) -> float:
@@ -78,6 +93,9 @@ class LinearGaussianLikelihood:
             raise ValueError("Phi must have one column per model dimension")
 
     def params(self, model) -> np.ndarray:
+        if model is not None and model.affine() is not None:
+            raise NotImplementedError("MultivariateNormalTriL priors are supported with the correlated-Gaussian "
+                                      "likelihood")
         return np.concatenate([self.Phi.ravel(), self.y, [self.sigma]]).astype(np.float32)
 
     def log_L_offset(self) -> float:

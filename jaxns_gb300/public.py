@@ -143,8 +143,10 @@ class UniDimSliceSampler:
             raise NotImplementedError("Adaptive shrinkage not implemented.")
         if not self.perfect:
             raise ValueError("Only perfect slice sampler is implemented.")
-        if self.gradient_slice:
-            raise NotImplementedError("gradient_slice (climb the gradient) is not on the fused GPU path")
+        self.gradient_slice = bool(self.gradient_slice)
+        if (self.gradient_slice or self.gradient_guided) and self.model.family not in (0, 1):
+            raise NotImplementedError("the gradient options of the slice sampler need the correlated-Gaussian or "
+                                      "Gaussian-shells likelihood (analytic U-space gradients)")
 
     def num_phantom(self) -> int:
         return self.num_phantom_save
@@ -203,7 +205,8 @@ class ShardedStaticNestedSampler:
                        init_efficiency_threshold=self.init_efficiency_threshold, store_U=self.store_U,
                        N=int(getattr(m.log_likelihood, "Phi", np.zeros((0, 0))).shape[0]),
                        log_L_offset=m.log_likelihood.log_L_offset(),
-                       gradient_guided=bool(getattr(self.sampler, "gradient_guided", False)))
+                       gradient_guided=bool(getattr(self.sampler, "gradient_guided", False)),
+                       gradient_slice=bool(getattr(self.sampler, "gradient_slice", False)))
 
     def _run(self, key, term_cond: TerminationCondition):
         batch = NSBatch([self.run_spec(key, term_cond)], device="cuda")

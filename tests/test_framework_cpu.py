@@ -74,3 +74,45 @@ def test_likelihood_dimension_check():
         yield gb.Prior(gb.Uniform(np.zeros(3), np.ones(3)), name="x")
     with pytest.raises(Exception):
         gb.Model(pm, gb.MultivariateNormalLikelihood(np.zeros(4), np.eye(4)))
+
+
+def test_multivariate_normal_tril_prior_and_fold():
+    """MultivariateNormalTriL prior: X = loc + L ndtri(U), log density of N(loc, L L^T), and the
+    folded correlated-Gaussian parameters give the likelihood of X exactly (FP64), mixed with a
+    Uniform block ahead of it."""
+    from scipy.special import ndtri
+    from scipy.stats import multivariate_normal
+    import jaxns_gb300 as gb
+    rng = np.random.default_rng(0)
+    D = 5
+    A = rng.standard_normal((D, D))
+    Lp = np.linalg.cholesky(A @ A.T / D + 0.3 * np.eye(D))
+    loc = rng.standard_normal(D)
+    mu = rng.standard_normal(D + 2)
+    B = rng.standard_normal((D + 2, D + 2))
+    cov = B @ B.T / D + 0.2 * np.eye(D + 2)
+
+    def prior_model():
+        a = yield gb.Prior(gb.Uniform(-2.0 * np.ones(2), 3.0 * np.ones(2)), name="a")
+        x = yield gb.Prior(gb.MultivariateNormalTriL(loc, Lp), name="x")
+        return a, x
+
+    lik = gb.MultivariateNormalLikelihood(mu, cov)
+    m = gb.Model(prior_model, lik)
+    U = rng.uniform(0.05, 0.95, size=(50, D + 2))
+    X = np.concatenate([-2.0 + 5.0 * U[:, :2], loc + ndtri(U[:, 2:]) @ Lp.T], 1)
+    np.testing.assert_allclose(m.transform_flat(U), X, rtol=0, atol=1e-12)
+    lp = np.log(1 / 5.0) * 2 + multivariate_normal(loc, Lp @ Lp.T).logpdf(X[:, 2:])
+    np.testing.assert_allclose(m.log_prob_prior(U), lp, rtol=1e-10)
+    # folded parameters, evaluated in FP64 on the kernels' per-dimension quantile outputs q
+    A_, c_ = m.affine()
+    Linv = np.linalg.inv(np.linalg.cholesky(cov))
+    mu_q = np.linalg.solve(A_, mu - c_)
+    q = np.concatenate([X[:, :2], ndtri(U[:, 2:])], 1)
+    z = (q - mu_q) @ np.tril(Linv @ A_).T
+    logL = -0.5 * np.sum(z * z, 1) + lik.log_L_offset()
+    np.testing.assert_allclose(logL, multivariate_normal(mu, cov).logpdf(X), rtol=1e-9)
+    p = m.family_params()  # the same fold, packed in fp32 for the device
+    np.testing.assert_allclose(p[:D + 2], mu_q, rtol=1e-5, atol=1e-5)
+    with pytest.raises(NotImplementedError):
+        gb.Model(prior_model, gb.GaussianShellsLikelihood(np.zeros(D + 2), np.ones(D + 2), 1.0, 0.1)).family_params()

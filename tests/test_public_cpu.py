@@ -70,8 +70,7 @@ def test_batched_sampler_assembles_one_run_per_problem():
 
 @pytest.mark.parametrize("kw,exc", [({"num_slices": 0}, ValueError), ({"num_phantom_save": -1}, ValueError),
                                     ({"num_phantom_save": 5}, ValueError), ({"perfect": False}, ValueError),
-                                    ({"adaptive_shrink": True}, NotImplementedError),
-                                    ({"gradient_slice": True}, NotImplementedError)])
+                                    ({"adaptive_shrink": True}, NotImplementedError)])
 def test_slice_sampler_validation(kw, exc):
     """samplers/uni_slice_sampler.py:276-326."""
     from jaxns_gb300.public import UniDimSliceSampler
@@ -79,6 +78,30 @@ def test_slice_sampler_validation(kw, exc):
     args.update(kw)
     with pytest.raises(exc):
         UniDimSliceSampler(**args)
+
+
+def test_slice_sampler_gradient_options():
+    """gradient_slice and gradient_guided reach the run spec (both kernels take them); the
+    linear-Gaussian family has no analytic U-space gradient on the device and refuses them."""
+    import jaxns_gb300 as gb
+    from jaxns_gb300.public import ShardedStaticNestedSampler, UniDimSliceSampler
+    m = _model(2)
+    smp = UniDimSliceSampler(model=m, num_slices=5, num_phantom_save=0, midpoint_shrink=True, perfect=True,
+                             gradient_slice=True)
+    ns = ShardedStaticNestedSampler(model=m, max_samples=1000, init_efficiency_threshold=0.1, sampler=smp,
+                                    num_live_points=20)
+    spec = ns.run_spec(gb.random.PRNGKey(0), gb.TerminationCondition())
+    assert spec.gradient_slice and not spec.gradient_guided
+    Phi = np.ones((4, 2))
+
+    def prior_model():
+        w = yield gb.Prior(gb.Normal(np.zeros(2), np.ones(2)), name="w")
+        return w
+
+    lg = gb.Model(prior_model, gb.LinearGaussianLikelihood(Phi, np.ones(4), 0.5))
+    with pytest.raises(NotImplementedError):
+        UniDimSliceSampler(model=lg, num_slices=5, num_phantom_save=0, midpoint_shrink=True, perfect=True,
+                           gradient_guided=True)
 
 
 def test_static_sampler_rounding():
