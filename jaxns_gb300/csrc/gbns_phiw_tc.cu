@@ -702,6 +702,48 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
   const float *pra = b.prior_a + rd.prior_off, *prb = b.prior_b + rd.prior_off;
   lf_cluster_sync();  // every CTA initialised before the first remote store
 
+  // ---- speculation.  Both possible continuations of a chain's next step are fixed by its
+  // keys, so each warp computes them while the cluster exchanges partial sums, off the critical
+  // path: the direction of the next slice (the normals of the current slice's after_key, lanes
+  // over dimensions), the keys and uniform of the next slice's first pick (B' = split(slices_key)[j],
+  // then run / t / after keys), and the keys and uniform of the next shrink step (from the
+  // current carry key).  The chain step then only selects.
+  float sa_va = 0.f, sa_vb = 0.f, sa_nrm = 1.f, sa_u = 0.f, sr_u = 0.f;
+  Key sa_ck = {0u, 0u}, sa_after = {0u, 0u}, sr_ck = {0u, 0u};
+  auto speculate = [&](Key next_dir_key, int next_j, Key cur_ck) {
+    if (P > 1) {
+      sa_va = ha ? normal_from_bits(bits64(next_dir_key, (uint32_t)pa_)) : 0.0f;
+      sa_vb = hb ? normal_from_bits(bits64(next_dir_key, (uint32_t)pb_)) : 0.0f;
+      sa_nrm = sqrtf(warp_sum(fmaf(sa_va, sa_va, sa_vb * sa_vb)));
+    }
+    // round 1 -- lane 0: B' = fold(slices_key, next_j); lane 1: shrink carry fold(ck, 0);
+    // lane 2: shrink t key fold(ck, 1)
+    const Key in1 = lane == 0 ? slices_key : cur_ck;
+    const uint32_t c1 = lane == 0 ? (uint32_t)next_j : (lane == 2 ? 1u : 0u);
+    uint32_t x0, x1;
+    threefry2x32(in1.k0, in1.k1, 0u, c1, x0, x1);
+    const Key Bn = {__shfl_sync(0xffffffffu, x0, 0), __shfl_sync(0xffffffffu, x1, 0)};
+    const Key tkr = {__shfl_sync(0xffffffffu, x0, 2), __shfl_sync(0xffffffffu, x1, 2)};
+    sr_ck.k0 = __shfl_sync(0xffffffffu, x0, 1);
+    sr_ck.k1 = __shfl_sync(0xffffffffu, x1, 1);
+    // round 2 -- lanes 0-2: the run, t and after keys of B' (counters 0, 2, 3); lane 3: the
+    // shrink step's 64 random bits
+    const Key in2 = lane == 3 ? tkr : Bn;
+    const uint32_t c2 = lane == 1 ? 2u : (lane == 2 ? 3u : 0u);
+    threefry2x32(in2.k0, in2.k1, 0u, c2, x0, x1);
+    sa_ck.k0 = __shfl_sync(0xffffffffu, x0, 0);
+    sa_ck.k1 = __shfl_sync(0xffffffffu, x1, 0);
+    const Key tka = {__shfl_sync(0xffffffffu, x0, 1), __shfl_sync(0xffffffffu, x1, 1)};
+    sa_after.k0 = __shfl_sync(0xffffffffu, x0, 2);
+    sa_after.k1 = __shfl_sync(0xffffffffu, x1, 2);
+    const uint32_t r0 = __shfl_sync(0xffffffffu, x0, 3), r1 = __shfl_sync(0xffffffffu, x1, 3);
+    sr_u = uniform01(((uint64_t)r0 << 32) | (uint64_t)r1);
+    // round 3 -- the first pick's 64 random bits
+    threefry2x32(tka.k0, tka.k1, 0u, 0u, x0, x1);
+    sa_u = uniform01(((uint64_t)x0 << 32) | (uint64_t)x1);
+  };
+  if (!(flags & LG_DONE)) speculate(dir_key, 0, ck);
+
   const int NMMA = R < 256 ? R : 256;
   const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NMMA >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
   const int nk8 = (P + 7) >> 3;
@@ -709,20 +751,21 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
   uint32_t mma_phase = 0;
   bool mma_pending = false;
   for (long long step = 0;; ++step) {
-    // ---- 1. chain step of the owned chain (k_lg_step)
+    // ---- 1. chain step of the owned chain (k_lg_step's logic, continuations precomputed)
     bool wrote = false;
     if (!(flags & LG_DONE)) {
+      bool start_now = true;  // the first pick of slice 0
       if (flags & LG_PENDING) {
-        double ss = 0.0;
-        if (lane == 0)
-          for (int src = 0; src < CS; ++src)
-            for (int h = 0; h < H; ++h) ss += slots[(src * H + h) * CPC + warp];
-        ss = __shfl_sync(0xffffffffu, ss, 0);
+        // this chain's residual sum: its partial sums from every CTA and column slice (one per
+        // lane), added in a fixed butterfly order
+        const double part_in = lane < CS * H ? slots[lane * CPC + warp] : 0.0;
+        const double ss = warp_sum(part_in);
         float logL = (float)(-ss * (double)inv2s2);  // relative to the run's log_L_offset
         if (logL != logL) logL = -INFINITY;
         ++total;
         ++in_slice;
         const bool accept = (logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar));
+        start_now = false;
         if (accept || in_slice >= b.max_evals_per_slice) {
           if (!accept) flags |= LG_FAILED;
           pair_add(ua, fmaf(t, da, la_), ua, la_);
@@ -736,15 +779,8 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
             if (lane == 0) b.ph_L[rd.phL_off + (size_t)c * K + ph] = logL;
           }
           ++j;
-          flags |= LG_START;
-          if (j < S) {
-            flags |= LG_NEED_DIR;
-            dir_key = after_key;
-          } else {
-            flags |= LG_DONE;
-          }
-        } else {
-          flags &= ~LG_START;
+          if (j < S) start_now = true;
+          else flags |= LG_DONE;
         }
         flags &= ~LG_PENDING;
       }
@@ -758,24 +794,17 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
           if (flags & LG_FAILED) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
         }
       } else {
-        if (flags & LG_NEED_DIR) {
+        float u;
+        if (start_now) {
           if (P == 1) {
             da = 1.0f;
           } else {
-            const float va = ha ? normal_from_bits(bits64(dir_key, (uint32_t)pa_)) : 0.0f;
-            const float vb = hb ? normal_from_bits(bits64(dir_key, (uint32_t)pb_)) : 0.0f;
-            const float nrm = sqrtf(warp_sum(fmaf(va, va, vb * vb)));
-            da = va / nrm;
-            db = vb / nrm;
+            da = sa_va / sa_nrm;
+            db = sa_vb / sa_nrm;
           }
-          flags &= ~LG_NEED_DIR;
-        }
-        const bool start = (flags & LG_START) != 0;
-        const Key B = start ? fold(slices_key, (uint32_t)j) : ck;
-        ck = fold(B, 0u);
-        const Key tk = fold(B, start ? 2u : 1u);
-        if (start) {
-          after_key = fold(B, 3u);
+          ck = sa_ck;
+          after_key = sa_after;
+          u = sa_u;
           alpha = lg_alpha(j, S);
           float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
 #pragma unroll
@@ -801,6 +830,8 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
           left = fmaxf(t0l, t1l);
           in_slice = 0;
         } else {
+          ck = sr_ck;
+          u = sr_u;
           if (t < 0.f) left = t;
           if (t > 0.f) right = t;
           if (rd.midpoint) {
@@ -808,7 +839,7 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
             if (t > 0.f) right = alpha * right;
           }
         }
-        t = fmaf(uniform01(bits64(tk, 0u)), right - left, left);
+        t = fmaf(u, right - left, left);
         // the proposal w as a TF32 hi / lo row of the W tile
         if (ha) {
           const float w = prior_quantile_pair(kind[pa_], pra[pa_], prb[pa_], ua, fmaf(t, da, la_));
@@ -829,16 +860,19 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
       }
     }
     __syncwarp();
-    if (wrote && lane < 16 * NKB) {
-      // copy the row (hi and lo, NKB blocks of 128 bytes) to the other CTAs of the cluster
-      const int blk = lane >> 3, chunk = lane & 7;
-      const uint32_t off = ((blk & 1) ? w_lo : w_hi) + (uint32_t)(blk >> 1) * 16384u + (uint32_t)crow * 128u +
-                           (uint32_t)chunk * 16u;
-      const uint4 v = *(const uint4 *)gptr(off);
-      for (int q = 0; q < CS; ++q)
-        if (q != (int)rank) lf_st_v4(lf_mapa(off, (uint32_t)q), v);
+    if (wrote) {
+      if (lane < 16 * NKB) {
+        // copy the row (hi and lo, NKB blocks of 128 bytes) to the other CTAs of the cluster
+        const int blk = lane >> 3, chunk = lane & 7;
+        const uint32_t off = ((blk & 1) ? w_lo : w_hi) + (uint32_t)(blk >> 1) * 16384u + (uint32_t)crow * 128u +
+                             (uint32_t)chunk * 16u;
+        const uint4 v = *(const uint4 *)gptr(off);
+        for (int q = 0; q < CS; ++q)
+          if (q != (int)rank) lf_st_v4(lf_mapa(off, (uint32_t)q), v);
+      }
+      // the tensor cores of every CTA read the row through the async proxy
+      asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
     }
-    asm volatile("fence.proxy.async.shared::cluster;" ::: "memory");
     const int act = __syncthreads_count(lane == 0 && !(flags & LG_DONE));
     if (tid < CS) lf_st_s32(lf_mapa(active_s + 4u * rank, (uint32_t)tid), abort_local ? LF_ABORT : act);
     lf_cluster_sync();  // (A) W tiles and active counts complete in every CTA
@@ -904,7 +938,11 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
       lf_st_f64(lf_mapa(slots_s + 8u * (uint32_t)(((int)rank * H + hs) * CPC + lc), (uint32_t)owner), part);
     }
     tc_fence_before();
-    lf_cluster_sync();  // (B) partial sums complete in their owners
+    // (B) partial sums complete in their owners; the continuations of the next step are
+    // computed between the arrival and the wait
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    if (flags & LG_PENDING) speculate(after_key, j + 1, ck);
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
   }
   // a timed-out MMA may still be in flight: give it one more bounded wait before the
   // tensor memory is released

@@ -26,12 +26,17 @@ struct RadixSmem {
   long long carry;
 };
 
+// LSD radix sort (4 x 8-bit digits of the upper 32 bits, stable by construction) of the
+// M keys in a, with tmp as the ping-pong buffer; sm.hist holds the digit histograms.  The
+// result is in a (an even number of passes).  blockDim.x must be 1024.
+__device__ void cta_radix_keys(long long M, unsigned long long *a, unsigned long long *tmp, RadixSmem &sm);
+
 // Stable ascending sort of the N+1 node keys (by their upper 32 bits).  Result in a (perm
 // in the low 32 bits).  a, tmp: [N+1] scratch.  blockDim.x must be 1024.
 __device__ unsigned long long *cta_sort_nodes(const float *L, long long N, unsigned long long *a,
                                               unsigned long long *tmp, RadixSmem &sm) {
   const long long M = N + 1;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   if (tid == 0) sm.flag = 1;
   for (int q = tid; q < 4 * 256; q += blockDim.x) (&sm.hist[0][0])[q] = 0;
   __syncthreads();
@@ -47,6 +52,12 @@ __device__ unsigned long long *cta_sort_nodes(const float *L, long long N, unsig
   if (!sorted) sm.flag = 0;
   __syncthreads();
   if (sm.flag) return a;
+  cta_radix_keys(M, a, tmp, sm);
+  return a;
+}
+
+__device__ void cta_radix_keys(long long M, unsigned long long *a, unsigned long long *tmp, RadixSmem &sm) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   unsigned long long *src = a, *dst = tmp;
   for (int d = 0; d < 4; ++d) {
     // exclusive prefix of the digit histogram
@@ -90,7 +101,6 @@ __device__ unsigned long long *cta_sort_nodes(const float *L, long long N, unsig
     src = dst;
     dst = t;
   }
-  return src;
 }
 
 // count_crossed_edges on one sample set (static variant).  perm: sorted node keys.
@@ -143,6 +153,117 @@ __global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const f
   __shared__ RadixSmem sm;
   unsigned long long *perm = cta_sort_nodes(L, N, scratch, scratch + (N + 1), sm);
   cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm);
+}
+
+// ---- count_crossed_edges of one large sample set over many CTAs ---------------------------
+//
+// A: node keys, sortedness, out-degrees (grid-wide; flag and degrees zeroed before);
+// B: one CTA radix-sorts the keys in place only when A found them out of order;
+// C: per chunk of the sorted order, the sum of (out-degree - 1);
+// D: one CTA turns the chunk sums into exclusive prefixes;
+// E: per chunk, the crossed-edge scan from its prefix and the outputs.
+// Every step is integer arithmetic, so the result is the single-CTA kernel's, bit for bit.
+constexpr int CE_CHUNK = 4096;  // sorted positions per CTA in C and E
+
+__global__ void __launch_bounds__(256) k_ce_keys(const int *sender, const float *L, long long N, unsigned long long *a,
+                                                 unsigned long long *flag, int *deg) {
+  const long long M = N + 1;
+  int unsorted = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const unsigned long long k = node_key(L, i);
+    a[i] = k;
+    if (i > 0 && (node_key(L, i - 1) >> 32) > (k >> 32)) unsorted = 1;
+    if (i < N) {
+      const int sd = max(sender[i], 0);
+      if ((long long)sd <= N) atomicAdd(&deg[sd], 1);
+    }
+  }
+  if (__any_sync(0xffffffffu, unsorted) && (threadIdx.x & 31) == 0) atomicOr(flag, 1ull);
+}
+
+__global__ void __launch_bounds__(1024) k_ce_sort(long long N, unsigned long long *a, unsigned long long *tmp,
+                                                  const unsigned long long *flag) {
+  __shared__ RadixSmem sm;
+  // every thread reads the flag before the first barrier, and the sort writes tmp (which
+  // holds the flag) only after it
+  if (*flag == 0ull) return;  // already in order (the usual case: dead points arrive sorted)
+  const long long M = N + 1;
+  for (int q = threadIdx.x; q < 4 * 256; q += blockDim.x) (&sm.hist[0][0])[q] = 0;
+  __syncthreads();
+  for (long long i = threadIdx.x; i < M; i += blockDim.x) {
+    const uint32_t key = (uint32_t)(a[i] >> 32);
+#pragma unroll
+    for (int d = 0; d < 4; ++d) atomicAdd(&sm.hist[d][(key >> (8 * d)) & 255], 1);
+  }
+  __syncthreads();
+  cta_radix_keys(M, a, tmp, sm);
+}
+
+__global__ void __launch_bounds__(256) k_ce_chunk_sums(long long N, const unsigned long long *perm, const int *deg,
+                                                       long long *bsum) {
+  __shared__ long long red[32];
+  const long long M = N + 1, i0 = (long long)blockIdx.x * CE_CHUNK;
+  long long v = 0;
+  for (long long i = i0 + threadIdx.x; i < min(M, i0 + CE_CHUNK); i += blockDim.x)
+    v += (long long)deg[(int)(perm[i] & 0xffffffffu)] - 1;
+  v = cta_sum_ll(v, red);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = v;
+}
+
+__global__ void __launch_bounds__(1024) k_ce_chunk_scan(long long *bsum, int nchunks) {
+  __shared__ long long wsum[32];
+  __shared__ long long carry;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = 1;  // crossed edges before the first node: the root's one edge
+  __syncthreads();
+  for (int c0 = 0; c0 < nchunks; c0 += blockDim.x) {
+    const int c = c0 + threadIdx.x;
+    const long long x = c < nchunks ? bsum[c] : 0;
+    long long v = warp_incl_scan(x);
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      long long y = wsum[lane];
+      y = warp_incl_scan(y);
+      wsum[lane] = y;
+    }
+    __syncthreads();
+    const long long incl = carry + v + (w > 0 ? wsum[w - 1] : 0);
+    if (c < nchunks) bsum[c] = incl - x;  // exclusive prefix, including the initial 1
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = incl;
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(1024) k_ce_chunk_out(long long N, const unsigned long long *perm, const int *deg,
+                                                       const long long *bsum, int *samples_indices, int *num_live) {
+  __shared__ long long wsum[32];
+  __shared__ long long carry;
+  const long long M = N + 1, i0 = (long long)blockIdx.x * CE_CHUNK, i1 = min(M, i0 + CE_CHUNK);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (threadIdx.x == 0) carry = bsum[blockIdx.x];
+  __syncthreads();
+  for (long long t0 = i0; t0 < i1; t0 += blockDim.x) {
+    const long long i = t0 + threadIdx.x;
+    const int node = i < i1 ? (int)(perm[i] & 0xffffffffu) : 0;
+    long long v = i < i1 ? (long long)deg[node] - 1 : 0;
+    v = warp_incl_scan(v);
+    if (lane == 31) wsum[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      long long y = wsum[lane];
+      y = warp_incl_scan(y);
+      wsum[lane] = y;
+    }
+    __syncthreads();
+    const long long crossed = carry + v + (w > 0 ? wsum[w - 1] : 0);
+    if (i < N && i < i1) num_live[i] = (int)crossed;
+    if (i >= 1 && i < i1) samples_indices[i - 1] = node - 1;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = crossed;
+    __syncthreads();
+  }
 }
 
 // compute_evidence_stats (internals/shrinkage_statistics.py:131-157) of one sample set on one
@@ -379,10 +500,31 @@ cudaError_t launch_results(const gbns_batch &b, const gbns_results_bufs &res, cu
   return cudaGetLastError();
 }
 
+// Up to CE_MULTI_MIN samples one CTA does everything; beyond, the work is spread over the grid
+// (scratch: 2 (N + 1) 64-bit words and N + 1 counters either way).
+constexpr long long CE_MULTI_MIN = 65536;
+
 cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long long N, int *samples_indices,
                                        int *num_live, long long *scratch_ll, int *scratch_i, cudaStream_t stream) {
-  k_count_edges<<<1, 1024, 0, stream>>>(sender, L, N, samples_indices, num_live, (unsigned long long *)scratch_ll,
-                                        scratch_i);
+  unsigned long long *a = (unsigned long long *)scratch_ll, *tmp = a + (N + 1);
+  if (N <= CE_MULTI_MIN) {
+    k_count_edges<<<1, 1024, 0, stream>>>(sender, L, N, samples_indices, num_live, a, scratch_i);
+    return cudaGetLastError();
+  }
+  // tmp[0] is A's out-of-order flag, then the sort's ping-pong buffer, then the chunk sums
+  cudaError_t e = cudaMemsetAsync(tmp, 0, sizeof(unsigned long long), stream);
+  if (e == cudaSuccess) e = cudaMemsetAsync(scratch_i, 0, sizeof(int) * (size_t)(N + 1), stream);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  k_ce_keys<<<sms * 8, 256, 0, stream>>>(sender, L, N, a, tmp, scratch_i);
+  k_ce_sort<<<1, 1024, 0, stream>>>(N, a, tmp, tmp);
+  const long long nchunks = (N + 1 + CE_CHUNK - 1) / CE_CHUNK;
+  long long *bsum = (long long *)tmp;
+  k_ce_chunk_sums<<<(unsigned)nchunks, 256, 0, stream>>>(N, a, scratch_i, bsum);
+  k_ce_chunk_scan<<<1, 1024, 0, stream>>>(bsum, (int)nchunks);
+  k_ce_chunk_out<<<(unsigned)nchunks, 1024, 0, stream>>>(N, a, scratch_i, bsum, samples_indices, num_live);
   return cudaGetLastError();
 }
 

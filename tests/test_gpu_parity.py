@@ -183,9 +183,12 @@ def test_count_crossed_edges_exact(gpu_lib, oracle_mod):
     L[:10] = 0.0
     L[10:20] = -0.0
     cases.append((sender, L))
-    N2 = 200000
+    N2 = 200000  # beyond 65536 samples the count runs over many CTAs: sorted, then unsorted with ties
     L2 = np.sort(rng.standard_normal(N2)).astype(np.float32)
     cases.append((np.minimum(np.arange(N2), rng.integers(0, N2, size=N2)), L2))
+    N3 = 300001
+    L3 = np.round(rng.standard_normal(N3), 3).astype(np.float32)
+    cases.append((rng.integers(-3, N3 + 5, size=N3), L3))
     for sender, L in cases:
         sender = np.asarray(sender, np.int32)
         L = np.asarray(L, np.float32)

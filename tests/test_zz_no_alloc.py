@@ -71,6 +71,7 @@ def test_static_scratch_matches_allocating_entry_point(gpu_lib, oracle_mod):
     cases = [(torch.tensor(s, device="cuda"), torch.tensor(L, device="cuda")) for s, L in host]
     # calls in a row on the shared scratch (each sees the previous call's leftovers), then the
     # first input again; both entry points against the oracle's count_crossed_edges
+    checked_first = False
     for k in list(range(len(cases))) + [0]:
         sender, L = cases[k]
         si_s, nl_s = _static(gpu_lib, sender, L)
@@ -78,7 +79,8 @@ def test_static_scratch_matches_allocating_entry_point(gpu_lib, oracle_mod):
         torch.cuda.synchronize()
         assert torch.equal(si_s, si_a)
         assert torch.equal(nl_s, nl_a)
-        if k in (0, 3):
+        if k != 0 or not checked_first:  # every case once (the large ones run over many CTAs)
+            checked_first = checked_first or k == 0
             osi, onl = oracle_mod.count_crossed_edges(host[k][0], host[k][1].astype(np.float64))
             np.testing.assert_array_equal(si_s.cpu().numpy(), osi)
             np.testing.assert_array_equal(nl_s.cpu().numpy(), onl)
