@@ -350,6 +350,17 @@ static double slice_alpha(int j, int S) {
 
 /* _new_proposal (uni_slice_sampler.py:114-273) with perfect=True, no gradient options.
  * U0/logL0 is the seed; on return U holds the accepted point, d the new direction. */
+/* When set (orc_slice_shell_margin), every accept test of the calling thread lowers
+ * *orc_margin_sink to |log L - L*|: how close the chain came to a tie with the contour. */
+static _Thread_local double *orc_margin_sink = NULL;
+
+static inline void note_margin(double logL, double Lstar) {
+    if (orc_margin_sink) {
+        double d = fabs(logL - Lstar);
+        if (!(d >= *orc_margin_sink)) *orc_margin_sink = d;
+    }
+}
+
 static double new_proposal(const orc_model *m, okey key, const double *U0, double logL0,
                            double *d, int midpoint, double alpha, double Lstar, double *U,
                            long *nevals, int gradient_guided, int gradient_slice) {
@@ -379,6 +390,7 @@ static double new_proposal(const orc_model *m, okey key, const double *U0, doubl
     double logL = orc_forward(m, U);
     ne += 1;
     okey ck = run_key;
+    note_margin(logL, Lstar);
     while (!((logL > Lstar) || ((logL0 == Lstar) && (logL == Lstar)))) {
         okey nk = key_fold(ck, 0);
         okey tk = key_fold(ck, 1);
@@ -391,6 +403,7 @@ static double new_proposal(const orc_model *m, okey key, const double *U0, doubl
         }
         t = pick_point(tk, U0, d, D, left, right, U);
         logL = orc_forward(m, U);
+        note_margin(logL, Lstar);
         ne += 1;
         ck = nk;
     }
@@ -1012,6 +1025,27 @@ void orc_slice_shell(const orc_model *m, const orc_slice_cfg *cfg, uint32_t k0, 
         okey kc = key_fold(key, (uint64_t)c);
         orc_slice_get_sample(m, cfg, kc.k0, kc.k1, Lstar, live_U, live_logL, n, U_out + c * D, &logL_out[c],
                              &nevals_out[c], pU, pL);
+    }
+    free(pU); free(pL);
+}
+
+/* orc_slice_shell that also reports, per chain, the smallest |log L - L*| over its accept
+ * tests: a chain of another implementation whose likelihoods differ by less than that from
+ * these FP64 ones makes every decision this chain makes. */
+void orc_slice_shell_margin(const orc_model *m, const orc_slice_cfg *cfg, uint32_t k0, uint32_t k1, double Lstar,
+                            const double *live_U, const double *live_logL, long n, long num_chains, double *U_out,
+                            double *logL_out, long *nevals_out, double *margin_out) {
+    okey key = {k0, k1};
+    int D = m->D, K = cfg->num_phantom;
+    double *pU = (double *)malloc(sizeof(double) * (size_t)(K > 0 ? K : 1) * D);
+    double *pL = (double *)malloc(sizeof(double) * (size_t)(K > 0 ? K : 1));
+    for (long c = 0; c < num_chains; ++c) {
+        okey kc = key_fold(key, (uint64_t)c);
+        margin_out[c] = INFINITY;
+        orc_margin_sink = &margin_out[c];
+        orc_slice_get_sample(m, cfg, kc.k0, kc.k1, Lstar, live_U, live_logL, n, U_out + c * D, &logL_out[c],
+                             &nevals_out[c], pU, pL);
+        orc_margin_sink = NULL;
     }
     free(pU); free(pL);
 }

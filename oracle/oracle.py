@@ -310,6 +310,25 @@ def slice_shell(model, key, L_star, live_U, live_logL, num_chains, num_slices, n
     return U, L, E
 
 
+def slice_shell_margin(model, key, L_star, live_U, live_logL, num_chains, num_slices, num_phantom=0,
+                       midpoint_shrink=True):
+    """slice_shell with, per chain, the smallest |log L - L*| over its accept tests (FP64)."""
+    D = model.D
+    live_U = np.ascontiguousarray(live_U, np.float64)
+    live_logL = np.ascontiguousarray(live_logL, np.float64)
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), 0, 0)
+    U = np.zeros((num_chains, D))
+    L = np.zeros(num_chains)
+    E = np.zeros(num_chains, np.int64)
+    M = np.zeros(num_chains)
+    m = model._c()
+    lib().orc_slice_shell_margin(ctypes.byref(m), ctypes.byref(cfg), ctypes.c_uint32(int(key[0])),
+                                 ctypes.c_uint32(int(key[1])), ctypes.c_double(L_star), _dp(live_U), _dp(live_logL),
+                                 ctypes.c_long(len(live_logL)), ctypes.c_long(num_chains), _dp(U), _dp(L), _lp(E),
+                                 _dp(M))
+    return U, L, E, M
+
+
 def uniform_get_sample(model, key, L_star, max_evals):
     U = np.zeros(model.D)
     logL = ctypes.c_double()

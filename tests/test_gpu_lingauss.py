@@ -40,9 +40,15 @@ def test_lingauss_forward(gpu_lib, oracle_mod):
     np.testing.assert_allclose(got, ref, rtol=1e-4, atol=5e-2)
 
 
-def test_lingauss_shell_chain_parity(gpu_lib, oracle_mod):
-    """One lock-step shell from the initial live set: same keys as the reference's
-    _collect_shell, chain by chain against the oracle."""
+@pytest.mark.parametrize("fused", [False, True])
+def test_lingauss_shell_chain_parity(gpu_lib, oracle_mod, fused):
+    """One shell from the initial live set (same keys as the reference's _collect_shell), chain by
+    chain against the FP64 oracle, through the two-launch lock step and through the fused shell.
+    Its residual sums come from 3xTF32 tensor-core products whose accumulation order is the
+    hardware's, so no model reproduces them bit for bit; instead the oracle reports for every
+    chain how close its likelihoods came to the contour, and every chain that never came within
+    the device's rounding band (1e-3 + 1e-5 |L*|: fp32 directions, pair arithmetic and fp32
+    residual tiles) makes the same decisions: the same evaluation count and the same point."""
     import jaxns_gb300 as gb
     from jaxns_gb300 import _ffi
     from jaxns_gb300.engine import NSBatch
@@ -52,7 +58,8 @@ def test_lingauss_shell_chain_parity(gpu_lib, oracle_mod):
     n, S = 100, 30
     ns = gb.NestedSampler(model, num_live_points=n, num_slices=S)
     spec = ns.nested_sampler.run_spec(gb.random.PRNGKey(9), ns.normalise_term_cond(None))
-    b = NSBatch([spec])
+    b = NSBatch([spec], lg_fused=fused)
+    assert b.lg_fused == fused
     b.init()
     live = b.live_view(0)
     K0 = np.array(b.state()[0]["key"], np.uint32)
@@ -60,19 +67,29 @@ def test_lingauss_shell_chain_parity(gpu_lib, oracle_mod):
     s = n // 2
     Lstar = float(live["log_L"][s - 1].item())
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    _ffi.call("gbns_lg_shell_begin", ctypes.byref(b._b), ctypes.byref(b._lgb), stream)
-    for _ in range(400):
-        _ffi.call("gbns_lg_steps", ctypes.byref(b._b), ctypes.byref(b._lgb), 16, stream)
-        if int(b.lg_t["chains_left"][0].item()) == 0:
-            break
+    if fused:
+        _ffi.call("gbns_lg_shell_fused", ctypes.byref(b._b), ctypes.byref(b._lgb), stream)
+    else:
+        _ffi.call("gbns_lg_shell_begin", ctypes.byref(b._b), ctypes.byref(b._lgb), stream)
+        for _ in range(400):
+            _ffi.call("gbns_lg_steps", ctypes.byref(b._b), ctypes.byref(b._lgb), 16, stream)
+            if int(b.lg_t["chains_left"][0].item()) == 0:
+                break
     torch.cuda.synchronize()
+    assert int(b.state()[0]["status"]) == 0
     om = oracle_mod.lingauss_model(Phi, y, 0.5, 1.0)
-    U_o, L_o, E_o = oracle_mod.slice_shell(om, sample_key, Lstar, live["U"].cpu().double().numpy(),
-                                           live["log_L"].cpu().double().numpy(), s, S)
+    U_o, L_o, E_o, M_o = oracle_mod.slice_shell_margin(om, sample_key, Lstar, live["U"].cpu().double().numpy(),
+                                                       live["log_L"].cpu().double().numpy(), s, S)
     E_g = b.new_E[:s].cpu().numpy()
     U_g = b.new_U_view(0).cpu().numpy()
     same = (E_g == E_o) & np.all(np.abs(U_g - U_o) < 2e-4, axis=1)
-    assert same.mean() >= 0.9, f"chain parity {same.mean():.3f}"
+    band = 1e-3 + 1e-5 * abs(Lstar)
+    clear = M_o > band
+    bad = np.nonzero(clear & ~same)[0]
+    assert len(bad) == 0, (f"chains {bad[:5]} differ although their FP64 likelihoods stayed farther than {band:.2e} "
+                           f"from the contour (margins {M_o[bad[:5]]})")
+    print(f"linear-Gaussian shell ({'fused' if fused else 'lock step'}): {np.count_nonzero(same)} of {s} chains "
+          f"equal to the FP64 oracle; {np.count_nonzero(~clear)} came within {band:.1e} of a tie")
 
 
 def test_lingauss_evidence_small(gpu_lib):

@@ -238,3 +238,22 @@ def test_grad_U_matches_finite_differences(oracle_mod):
             fd = np.array([(oracle_mod.forward(m, (U + h * e)[None])[0] - oracle_mod.forward(m, (U - h * e)[None])[0])
                            / (2 * h) for e in np.eye(D)])
             np.testing.assert_allclose(g, fd, rtol=1e-5, atol=1e-6 * max(1.0, np.abs(fd).max()))
+
+
+def test_slice_shell_margin_reports_closest_approach(oracle_mod):
+    """The margin-reporting shell runs the same chains as slice_shell, and every margin is the
+    smallest |log L - L*| over the chain's accept tests (non-negative, finite)."""
+    from tests.conftest import corr_gauss
+    D = 4
+    mu, cov = corr_gauss(D, 1)
+    om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    U = np.random.default_rng(0).uniform(size=(200, D))
+    L = oracle_mod.forward(om, U)
+    o = np.argsort(L)
+    U, L = U[o], L[o]
+    U1, L1, E1, M1 = oracle_mod.slice_shell_margin(om, oracle_mod.PRNGKey(3), L[99], U, L, 100, 8)
+    U0, L0, E0 = oracle_mod.slice_shell(om, oracle_mod.PRNGKey(3), L[99], U, L, 100, 8)
+    np.testing.assert_array_equal(E1, E0)
+    np.testing.assert_array_equal(U1, U0)
+    assert np.all(np.isfinite(M1)) and np.all(M1 >= 0)
+    assert np.all(M1 <= np.abs(L1 - L[99]) + 1e-12)  # the accepted point itself is one of the tests
