@@ -483,7 +483,7 @@ def round_up_max_samples(max_samples, num_discard, num_phantom):
 def ns_run(model: OracleModel, key, num_live_points, num_slices, max_samples=None, num_phantom=0,
            midpoint_shrink=True, shell_fraction=0.5, init_efficiency_threshold=0.1,
            term_cond: Optional[dict] = None, max_iterations=0, init_only=False,
-           gradient_guided=False) -> OracleRun:
+           gradient_guided=False, gradient_slice=False) -> OracleRun:
     """NestedSampler(...)(key, term_cond) followed by to_results(trim=True)."""
     shell_fraction = max(shell_fraction, 1.0 / num_live_points)
     n = round_up_num_live_points(num_live_points, shell_fraction)
@@ -496,7 +496,8 @@ def ns_run(model: OracleModel, key, num_live_points, num_slices, max_samples=Non
     tc["max_samples"] = min(float(tc.get("max_samples") or big), float(cap))
     cfg = _NSCfg(n, s, cap, float(init_efficiency_threshold), _SliceCfg(num_slices, num_phantom,
                                                                       int(midpoint_shrink),
-                                                                      int(gradient_guided)), 100)
+                                                                      int(gradient_guided),
+                                                                      int(gradient_slice)), 100)
     D = model.D
     sender = np.zeros(cap, np.int64)
     log_L = np.zeros(cap)

@@ -294,9 +294,14 @@ def test_gradient_slice_shells_exact(gpu_lib, oracle_mod):
     assert_shell_exact(oracle_mod, b, 0, Ls, key)
 
 
-def test_gradient_slice_log_Z(gpu_lib):
+def test_gradient_slice_run_matches_oracle(gpu_lib, oracle_mod):
     """ShardedStaticNestedSampler with UniDimSliceSampler(gradient_slice=True) end to end on a
-    correlated Gaussian (D = 5): log Z within 4 sigma of the analytic value."""
+    correlated Gaussian (D = 5).  The reference offers gradient_slice for global optimisation
+    (experimental/public.py:44-77): every slice starts from its seed along the normalised
+    gradient with the left end at the seed, a climb that does not leave the constrained prior
+    invariant.  Its evidence is therefore biased (about +8 nats here, in the FP64 oracle as on
+    the device), so the run is checked against the FP64 oracle's run of the same algorithm and
+    for what the option is for: the maximum likelihood it reaches."""
     import jaxns_gb300 as gb
     from jaxns_gb300.public import ShardedStaticNestedSampler, UniDimSliceSampler
     D = 5
@@ -314,7 +319,15 @@ def test_gradient_slice_log_Z(gpu_lib):
                                     num_live_points=300)
     reason, batch = ns._run(gb.random.PRNGKey(9), gb.TerminationCondition(dlogZ=1e-4))
     sc = batch.results(with_U=False)["scalars"].cpu().numpy()[0]
-    assert abs(sc[0] + D * np.log(20.0)) < 4 * sc[1] + 0.02, (sc[0], sc[1])
+    om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    r = oracle_mod.ns_run(om, oracle_mod.PRNGKey(9), 300, 5 * D, max_samples=100000,
+                          term_cond={"dlogZ": 1e-4}, gradient_slice=True)
+    ref, ref_unc = r.results["log_Z_mean"], r.results["log_Z_uncert"]
+    assert abs(sc[0] - ref) < 4 * np.hypot(sc[1], ref_unc) + 0.05, (sc[0], sc[1], ref, ref_unc)
+    # the climb reaches the likelihood's peak: log L_max = -0.5 log det(2 pi cov)
+    peak = -0.5 * np.linalg.slogdet(2 * np.pi * cov)[1]
+    top = float(batch.live_view(0)["log_L"].max().item())
+    assert top > peak - 1e-3, (top, peak)
 
 
 def test_gradient_guided_log_Z(gpu_lib):
