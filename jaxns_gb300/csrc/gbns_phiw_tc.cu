@@ -532,9 +532,10 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
 //      leaves the loop when none is left;
 //   3. one thread issues the 3xTF32 tcgen05 MMAs of W (128 chains) x Phi slice (R rows);
 //   4. every warp drains a lane quarter x column slice of the accumulator (thread = chain),
-//      sums (y - Phi w)^2 over its rows and stores the partial sum in the owner CTA's shared
-//      memory; cluster barrier.
-// The owner adds a chain's partial sums in rank order, so the sum is deterministic.  Every
+//      sums (y - Phi w)^2 over its rows (fp32 over 32-row chunks, the chunks as an fp32
+//      pair) and stores the partial sum in the owner CTA's shared memory; cluster barrier.
+// The owner adds a chain's partial sums in a fixed butterfly order, so the sum is
+// deterministic.  Every
 // mbarrier wait is bounded: a CTA whose wait timed out reports it through its active count,
 // every CTA of the cluster then leaves at the same barrier, and the run's status gets
 // GBNS_ERR_WAIT_TIMEOUT.
@@ -572,8 +573,18 @@ __device__ __forceinline__ void lf_st_v4(uint32_t addr, uint4 v) {
                : "memory");
 }
 
-__device__ __forceinline__ void lf_st_f64(uint32_t addr, double v) {
-  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(addr), "d"(v) : "memory");
+__device__ __forceinline__ void lf_st_f32x2(uint32_t addr, float a, float b) {
+  asm volatile("st.shared::cluster.v2.f32 [%0], {%1, %2};" ::"r"(addr), "f"(a), "f"(b) : "memory");
+}
+
+// hi + lo += x (TwoSum of hi and x, the rounding error carried in lo).  GB300 runs FP64 at
+// about 1/64 of the FP32 rate, so the step's sums of squares travel as fp32 pairs: each adds
+// at most a few units of 2^-48 of relative error, far below the fp32 rounding of the 32-row
+// chunk sums they carry.
+__device__ __forceinline__ void lf_pair_acc(float &hi, float &lo, float x) {
+  float e;
+  pair_add(hi, x, hi, e);
+  lo += e;
 }
 
 __device__ __forceinline__ void lf_st_s32(uint32_t addr, int v) {
@@ -612,11 +623,12 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
   const uint32_t phi_hi = base, phi_lo = base + (uint32_t)(NKB * R * 128);
   const uint32_t w_hi = base + (uint32_t)(2 * NKB * R * 128), w_lo = w_hi + (uint32_t)(NKB * 16384);
   const uint32_t ys_s = w_lo + (uint32_t)(NKB * 16384);
-  const uint32_t slots_s = ys_s + (uint32_t)(R * 4);                  // double [CS][H][CPC]
+  const uint32_t slots_s = ys_s + (uint32_t)(R * 4);                  // float2 [CS][H][CPC]
   const uint32_t active_s = slots_s + (uint32_t)(CS * H * CPC * 8);   // int [CS]
+  // slots: fp32 pairs (hi, lo) [CS][H][CPC]
   auto gptr = [&](uint32_t sa) { return (void *)(lf_dyn + (sa - dyn0)); };
   float *ys = (float *)gptr(ys_s);
-  const double *slots = (const double *)gptr(slots_s);
+  const float2 *slots = (const float2 *)gptr(slots_s);
   const int *active_in = (const int *)gptr(active_s);
   const uint32_t bar_phi = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
 
@@ -708,39 +720,43 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
   // over dimensions), the keys and uniform of the next slice's first pick (B' = split(slices_key)[j],
   // then run / t / after keys), and the keys and uniform of the next shrink step (from the
   // current carry key).  The chain step then only selects.
+  // The next slice's continuation (its direction normals from this slice's after_key, its base
+  // key B' and the keys and uniform of its first pick) is the same for every step of a slice:
+  // it is derived at the slice's first step (spec_j records for which slice) and reused; only
+  // the shrink continuation changes from step to step.
   float sa_va = 0.f, sa_vb = 0.f, sa_nrm = 1.f, sa_u = 0.f, sr_u = 0.f;
   Key sa_ck = {0u, 0u}, sa_after = {0u, 0u}, sr_ck = {0u, 0u};
+  int spec_j = -1;
   auto speculate = [&](Key next_dir_key, int next_j, Key cur_ck) {
-    if (P > 1) {
-      sa_va = ha ? normal_from_bits(bits64(next_dir_key, (uint32_t)pa_)) : 0.0f;
-      sa_vb = hb ? normal_from_bits(bits64(next_dir_key, (uint32_t)pb_)) : 0.0f;
-      sa_nrm = sqrtf(warp_sum(fmaf(sa_va, sa_va, sa_vb * sa_vb)));
-    }
-    // round 1 -- lane 0: B' = fold(slices_key, next_j); lane 1: shrink carry fold(ck, 0);
-    // lane 2: shrink t key fold(ck, 1)
-    const Key in1 = lane == 0 ? slices_key : cur_ck;
-    const uint32_t c1 = lane == 0 ? (uint32_t)next_j : (lane == 2 ? 1u : 0u);
     uint32_t x0, x1;
-    threefry2x32(in1.k0, in1.k1, 0u, c1, x0, x1);
-    const Key Bn = {__shfl_sync(0xffffffffu, x0, 0), __shfl_sync(0xffffffffu, x1, 0)};
-    const Key tkr = {__shfl_sync(0xffffffffu, x0, 2), __shfl_sync(0xffffffffu, x1, 2)};
+    if (next_j != spec_j) {
+      spec_j = next_j;
+      if (P > 1) {
+        sa_va = ha ? normal_from_bits(bits64(next_dir_key, (uint32_t)pa_)) : 0.0f;
+        sa_vb = hb ? normal_from_bits(bits64(next_dir_key, (uint32_t)pb_)) : 0.0f;
+        sa_nrm = sqrtf(warp_sum(fmaf(sa_va, sa_va, sa_vb * sa_vb)));
+      }
+      // B' = fold(slices_key, next_j); then lanes 0-2: its run, t and after keys (counters
+      // 0, 2, 3); then the first pick's 64 random bits
+      threefry2x32(slices_key.k0, slices_key.k1, 0u, (uint32_t)next_j, x0, x1);
+      const uint32_t c2 = lane == 1 ? 2u : (lane == 2 ? 3u : 0u);
+      threefry2x32(x0, x1, 0u, c2, x0, x1);
+      sa_ck.k0 = __shfl_sync(0xffffffffu, x0, 0);
+      sa_ck.k1 = __shfl_sync(0xffffffffu, x1, 0);
+      const Key tka = {__shfl_sync(0xffffffffu, x0, 1), __shfl_sync(0xffffffffu, x1, 1)};
+      sa_after.k0 = __shfl_sync(0xffffffffu, x0, 2);
+      sa_after.k1 = __shfl_sync(0xffffffffu, x1, 2);
+      threefry2x32(tka.k0, tka.k1, 0u, 0u, x0, x1);
+      sa_u = uniform01(((uint64_t)x0 << 32) | (uint64_t)x1);
+    }
+    // the shrink continuation -- lane 1: carry fold(ck, 0); lane 2: t key fold(ck, 1); then
+    // the t key's 64 random bits
+    threefry2x32(cur_ck.k0, cur_ck.k1, 0u, lane == 2 ? 1u : 0u, x0, x1);
     sr_ck.k0 = __shfl_sync(0xffffffffu, x0, 1);
     sr_ck.k1 = __shfl_sync(0xffffffffu, x1, 1);
-    // round 2 -- lanes 0-2: the run, t and after keys of B' (counters 0, 2, 3); lane 3: the
-    // shrink step's 64 random bits
-    const Key in2 = lane == 3 ? tkr : Bn;
-    const uint32_t c2 = lane == 1 ? 2u : (lane == 2 ? 3u : 0u);
-    threefry2x32(in2.k0, in2.k1, 0u, c2, x0, x1);
-    sa_ck.k0 = __shfl_sync(0xffffffffu, x0, 0);
-    sa_ck.k1 = __shfl_sync(0xffffffffu, x1, 0);
-    const Key tka = {__shfl_sync(0xffffffffu, x0, 1), __shfl_sync(0xffffffffu, x1, 1)};
-    sa_after.k0 = __shfl_sync(0xffffffffu, x0, 2);
-    sa_after.k1 = __shfl_sync(0xffffffffu, x1, 2);
-    const uint32_t r0 = __shfl_sync(0xffffffffu, x0, 3), r1 = __shfl_sync(0xffffffffu, x1, 3);
-    sr_u = uniform01(((uint64_t)r0 << 32) | (uint64_t)r1);
-    // round 3 -- the first pick's 64 random bits
-    threefry2x32(tka.k0, tka.k1, 0u, 0u, x0, x1);
-    sa_u = uniform01(((uint64_t)x0 << 32) | (uint64_t)x1);
+    const Key tkr = {__shfl_sync(0xffffffffu, x0, 2), __shfl_sync(0xffffffffu, x1, 2)};
+    threefry2x32(tkr.k0, tkr.k1, 0u, 0u, x0, x1);
+    sr_u = uniform01(((uint64_t)x0 << 32) | (uint64_t)x1);
   };
   if (!(flags & LG_DONE)) speculate(dir_key, 0, ck);
 
@@ -758,9 +774,18 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
       if (flags & LG_PENDING) {
         // this chain's residual sum: its partial sums from every CTA and column slice (one per
         // lane), added in a fixed butterfly order
-        const double part_in = lane < CS * H ? slots[lane * CPC + warp] : 0.0;
-        const double ss = warp_sum(part_in);
-        float logL = (float)(-ss * (double)inv2s2);  // relative to the run's log_L_offset
+        const float2 part_in = lane < CS * H ? slots[lane * CPC + warp] : make_float2(0.0f, 0.0f);
+        float shi = part_in.x, slo = part_in.y;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          const float ohi = __shfl_xor_sync(0xffffffffu, shi, o), olo = __shfl_xor_sync(0xffffffffu, slo, o);
+          float e;
+          pair_add(shi, ohi, shi, e);
+          slo = (slo + olo) + e;
+        }
+        // -(shi + slo) * inv2s2, the product's rounding error carried by an FMA
+        const float prod = shi * inv2s2;
+        float logL = -(prod + fmaf(slo, inv2s2, fmaf(shi, inv2s2, -prod)));  // relative to log_L_offset
         if (logL != logL) logL = -INFINITY;
         ++total;
         ++in_slice;
@@ -906,7 +931,7 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
       tc_commit(bar_mma);
     }
     // ---- 3. epilogue: this warp's 32 chains x its column slice
-    double part = 0.0;
+    float part = 0.0f, part_lo = 0.0f;
     if (nbox > 0) {
       bool ok = mbar_wait(bar_mma, mma_phase);
       ok = __syncthreads_and(ok);
@@ -928,14 +953,15 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
             const float rr = ys[col + q] - v[q];
             p = (col + q < cend) ? fmaf(rr, rr, p) : p;
           }
-          part += (double)p;
+          lf_pair_acc(part, part_lo, p);
         }
       }
     }
     {
       const int row_c = qd * 32 + lane;  // chain row of this thread's accumulator lane
       const int owner = row_c / CPC, lc = row_c - owner * CPC;
-      lf_st_f64(lf_mapa(slots_s + 8u * (uint32_t)(((int)rank * H + hs) * CPC + lc), (uint32_t)owner), part);
+      lf_st_f32x2(lf_mapa(slots_s + 8u * (uint32_t)(((int)rank * H + hs) * CPC + lc), (uint32_t)owner), part,
+                  part_lo);
     }
     tc_fence_before();
     // (B) partial sums complete in their owners; the continuations of the next step are
