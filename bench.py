@@ -248,6 +248,29 @@ def cpu_runs_per_s(wl, name, threads):
 
 # ----------------------------------------------------------------- main
 
+def plain_sample(Ds, strata: int = 8):
+    """Runs for the plain single-run comparison: the batch's dimensions split into `strata`
+    equal-width ranges; per non-empty range the run whose D is nearest the range's median D,
+    weighted by the number of runs in the range (the weights sum to the batch size).  A batch
+    of one dimension gives `strata` evenly spaced runs of equal weight."""
+    Ds = np.asarray(Ds)
+    R = len(Ds)
+    lo, hi = int(Ds.min()), int(Ds.max())
+    if lo == hi:
+        idx = list(range(0, R, max(1, R // strata)))
+        return idx, [R / len(idx)] * len(idx)
+    edges = np.linspace(lo, hi + 1, strata + 1)
+    idx, weight = [], []
+    for a, b_ in zip(edges[:-1], edges[1:]):
+        members = np.nonzero((Ds >= a) & (Ds < b_))[0]
+        if len(members) == 0:
+            continue
+        med = np.median(Ds[members])
+        idx.append(int(members[np.argmin(np.abs(Ds[members] - med))]))
+        weight.append(float(len(members)))
+    return idx, weight
+
+
 def flops_per_eval(D, kind):
     """Algorithmic FP32 flops of one likelihood evaluation: MVN D^2 + 8D (proposal, prior
     quantile, triangular solve, sum of squares; the TriL prior's matvec is folded into the
@@ -499,22 +522,29 @@ def main():
             "iterations": {"max": int(st["iterations"].max()), "mean": float(st["iterations"].mean())}}
 
     if rank == 0 and not args.no_plain:
-        # plain single-run GPU kernel loop: runs one at a time, eager launches, no graph
+        # plain single-run GPU kernel loop: runs one at a time, eager launches, no graph, on a
+        # sample stratified by dimension (a run's cost grows steeply with D), each sampled run
+        # standing for the runs of its stratum
         from jaxns_gb300.engine import NSBatch
-        idx = list(range(0, args.runs, max(1, args.runs // 8)))
-        tot = 0.0
-        for r in idx:
+        idx, weight = plain_sample([w[0] for w in wl])
+        tot, est = 0.0, 0.0
+        for r, wt in zip(idx, weight):
             one = NSBatch([b.specs[r]])
             torch.cuda.synchronize()
             t0 = time.time()
             one.run(block=1, use_graph=False)
             one.results(with_U=False)
             torch.cuda.synchronize()
-            tot += time.time() - t0
+            dt = time.time() - t0
+            tot += dt
+            est += wt * dt
             del one
-        plain = len(idx) / tot
-        line["plain_single_run_loop"] = {"runs_per_s": plain, "sample": f"{len(idx)} runs one at a time, eager launches",
-                                         "batched_speedup": value / world / plain}
+        plain = len(wl) / est
+        line["plain_single_run_loop"] = {
+            "runs_per_s": plain, "batched_speedup": value / world / plain,
+            "sample": f"{len(idx)} runs one at a time, eager launches ({tot:.1f} s); runs with D "
+                      f"{[int(wl[r][0]) for r in idx]}, each weighted by the runs of its stratum "
+                      f"{[int(v) for v in weight]} (equal-width strata of D)"}
     if rank == 0 and args.workload == "shells" and not args.no_adjoint:
         line["adjoint"] = adjoint_record()
     if rank == 0 and not args.no_cpu:

@@ -174,10 +174,11 @@ typedef struct {
     int max_evals_per_slice;        /* shrink-loop evaluation budget per slice */
     int gradient_guided;            /* UniDimSliceSampler(gradient_guided=True): after each accepted point
                                        the direction is reflected about the U-space gradient of log L
-                                       (MVN and shells families) */
+                                       (every family; the linear-Gaussian family on its lock step) */
     int gradient_slice;             /* UniDimSliceSampler(gradient_slice=True): every slice runs along the
                                        normalised U-space gradient at its seed point, t in [0, right]
-                                       (one extra evaluation per slice; MVN and shells families) */
+                                       (one extra evaluation per slice; every family, the linear-Gaussian
+                                       family on its lock step) */
 } gbns_batch;
 
 /* Lock-step chain state of the linear-Gaussian family (device, caller-allocated).  Its
@@ -229,6 +230,13 @@ typedef struct {
     int rows_per_cta;                       /* 128, 256 or 512; rows_per_cta * ceil(pmax / 32) <= 512 */
     int pad_fused;
     long long max_steps;                    /* lock-step budget of one shell (sets GBNS_ERR_SHRINK_BUDGET) */
+    /* The slice sampler's gradient options (gbns_batch.gradient_guided / gradient_slice) on the
+     * lock step: a chain that needs the U-space gradient at its point sits out one step while
+     * a gradient launch computes Phi^T (y - Phi w) / sigma^2 times dw/du for every listed chain.
+     * Not used by the fused shell. */
+    float *grad;                            /* [sum s * D] the gradient of each listed chain */
+    long long *grad_list;                   /* [sum s] chains that asked for a gradient this step */
+    int *grad_count;                        /* [1] entries of grad_list (zeroed before each chain step) */
 } gbns_lg_bufs;
 
 /* results buffers (device) */

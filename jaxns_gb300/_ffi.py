@@ -75,7 +75,8 @@ class LGBufs(ctypes.Structure):
                 ("row_base", c_void_p), ("total_rows", c_ll), ("num_ctas_tc", c_int), ("num_tiles", c_int),
                 ("chain_run", c_void_p), ("tile_base", c_void_p), ("tile_pending", c_void_p), ("tc_done", c_void_p),
                 ("items_fused", c_void_p), ("num_items_fused", c_int), ("cluster_size", c_int),
-                ("rows_per_cta", c_int), ("pad_fused", c_int), ("max_steps", c_ll)]
+                ("rows_per_cta", c_int), ("pad_fused", c_int), ("max_steps", c_ll),
+                ("grad", c_void_p), ("grad_list", c_void_p), ("grad_count", c_void_p)]
 
 
 class ResultsBufs(ctypes.Structure):

@@ -182,12 +182,13 @@ __device__ __forceinline__ int cta_and(int v, int *red) {
 //   A_k  = ZX_k / X_k = A_{k-1} + X2_{k-1} tT_k mid_k / X_k              (an exclusive prefix sum)
 //   Z2_k = Z2_{k-1} + 2 X_{k-1} A_{k-1} t_k mid_k + X2_{k-1} t2_k mid_k^2
 //   dZ2_k = dZ2_{k-1} + X2_{k-1} t2_k mid_k^2
-// Every term is held as a scaled sum q 2^e: an exact power of two from the FP64 log-value and
-// an fp32-accurate mantissa, so no term loses relative precision however far it lies below
-// the others; sums are FP64 mantissas rescaled exactly by powers of two.  Z, Z2 and dZ2 are
-// accumulated per thread and reduced once at the end; log X, log X2 and A are CTA scans with
-// carries between chunks.  Coefficients per n come from an FP64 table built on the host with
-// the reference formulas.
+// Every term is held as a scaled sum q 2^e: an exact power of two from the log-value and an
+// fp32-accurate mantissa, so no term loses relative precision however far it lies below the
+// others.  Inside a chunk of blockDim elements the terms and their sums are fp32 pairs (FS,
+// below); the accumulators carried from chunk to chunk are FP64 mantissas (ScaledSum), both
+// rescaled exactly by powers of two.  Z, Z2 and dZ2 are accumulated per thread and reduced
+// once at the end; log X and log X2 (FP64) and A are CTA scans with carries between chunks.
+// Coefficients per n come from an FP64 table built on the host with the reference formulas.
 
 struct ScaledSum {
   double q;
@@ -217,17 +218,6 @@ __device__ __forceinline__ ScaledSum ss_from_log(double lv) {
   return s;
 }
 
-// exp(lv) as one term of a sum: exact power of two, mantissa in [1, 2) to fp32 precision
-__device__ __forceinline__ ScaledSum ss_term(double lv) {
-  ScaledSum s;
-  if (!(lv > -1e300)) { s.q = 0.0; s.e = 0; return s; }
-  const double y = lv * GBNS_INV_LN2;
-  const double f = floor(y);
-  s.q = (double)exp2f((float)(y - f));
-  s.e = (int)f;
-  return s;
-}
-
 __device__ __forceinline__ double ss_log(ScaledSum s) {
   if (!(s.q > 0.0)) return -INFINITY;
   return log(s.q) + (double)s.e * GBNS_LN2;
@@ -248,24 +238,8 @@ __device__ __forceinline__ ScaledSum ss_sum(ScaledSum a, ScaledSum b) {
   return r;
 }
 
-__device__ __forceinline__ ScaledSum shfl_up_ss(ScaledSum v, int o) {
-  ScaledSum r;
-  r.q = __shfl_up_sync(0xffffffffu, v.q, o);
-  r.e = __shfl_up_sync(0xffffffffu, v.e, o);
-  return r;
-}
-
-__device__ __forceinline__ ScaledSum shfl_xor_ss(ScaledSum v, int o) {
-  ScaledSum r;
-  r.q = __shfl_xor_sync(0xffffffffu, v.q, o);
-  r.e = __shfl_xor_sync(0xffffffffu, v.e, o);
-  return r;
-}
-
 struct EvScanSmem {
   double wa[32], wb[32];
-  ScaledSum ws[32];
-  ScaledSum red[3][32];
   double last_ldZ;
   float last_L;
 };
@@ -308,35 +282,6 @@ __device__ __forceinline__ void cta_scan_d2(double &a, double &b, double &ta, do
   }
   ta = sm.wa[nw - 1];
   tb = sm.wb[nw - 1];
-  __syncthreads();
-}
-
-// CTA scan of scaled sums: inclusive and exclusive prefix of each thread's value, and the total.
-__device__ __forceinline__ void cta_scan_ss(ScaledSum v, ScaledSum &incl, ScaledSum &excl, ScaledSum &tot,
-                                            EvScanSmem &sm) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const ScaledSum u = shfl_up_ss(v, o);
-    if (lane >= o) v = ss_sum(u, v);
-  }
-  ScaledSum wex = shfl_up_ss(v, 1);
-  if (lane == 31) sm.ws[w] = v;
-  __syncthreads();
-  if (w == 0) {
-    ScaledSum x = lane < nw ? sm.ws[lane] : ss_zero();
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const ScaledSum u = shfl_up_ss(x, o);
-      if (lane >= o) x = ss_sum(u, x);
-    }
-    if (lane < nw) sm.ws[lane] = x;
-  }
-  __syncthreads();
-  const ScaledSum pw = w > 0 ? sm.ws[w - 1] : ss_zero();
-  incl = ss_sum(pw, v);
-  excl = lane == 0 ? pw : ss_sum(pw, wex);
-  tot = sm.ws[nw - 1];
   __syncthreads();
 }
 
@@ -392,6 +337,158 @@ __device__ __forceinline__ void ncoef_compute(double n, double *c) {
   c[4] = -lae(0.0, -lnn) - lnn2;
 }
 
+// ---- fp32-pair scaled sums.  GB300 runs FP64 at about 1/64 of the FP32 rate, so inside a
+// scan only the log-X prefix (which must stay within 1e-12 of the reference's FP64 values) is
+// FP64; every exponential term and every sum of terms is an fp32 pair (h + l) 2^e: TwoSum
+// additions (relative error a few units of 2^-48), exponents aligned by exact powers of two.
+// The terms themselves carry fp32 mantissas (exp2f of a pair-accurate fraction), as the FP64
+// scaled sums do.  Chunk totals are folded into the FP64 accumulators once per chunk.
+struct FS {
+  float h, l;
+  int e;  // value = (h + l) 2^e, h == 0 means zero
+};
+
+__device__ __forceinline__ FS fs_zero() {
+  FS s;
+  s.h = 0.0f;
+  s.l = 0.0f;
+  s.e = 0;
+  return s;
+}
+
+__device__ __forceinline__ void pair_sum2(float ah, float al, float bh, float bl, float &h, float &l) {
+  const float s = ah + bh;
+  const float bb = s - ah;
+  const float err = (ah - (s - bb)) + (bh - bb);
+  const float lo = (al + bl) + err;
+  h = s + lo;
+  l = lo - (h - s);
+}
+
+// an FP64 value as an fp32 pair
+__device__ __forceinline__ void pair_of(double x, float &h, float &l) {
+  h = __double2float_rn(x);
+  l = (isinf(h) || isnan(h)) ? 0.0f : __double2float_rn(x - (double)h);
+}
+
+// exp(vh + vl): an exact power of two times exp2f of the fraction (vh + vl) / ln 2 - e
+__device__ __forceinline__ FS fs_term(float vh, float vl) {
+  if (!(vh > -INFINITY) || !(vh < INFINITY)) return fs_zero();  // -inf, +inf or NaN: no term
+  const float c_hi = 1.44269502162933349609375f, c_lo = 1.925963033500011079e-8f;  // 1/ln 2 as a pair
+  const float p = vh * c_hi;
+  const float pe = fmaf(vh, c_hi, -p) + fmaf(vh, c_lo, vl * c_hi);
+  const float f = floorf(p);
+  FS s;
+  s.h = exp2f((p - f) + pe);
+  s.l = 0.0f;
+  s.e = (int)f;
+  return s;
+}
+
+// a + b (commutative: the operand with the larger exponent is always the first)
+__device__ __forceinline__ FS fs_sum(FS a, FS b) {
+  if (!(b.h > 0.0f)) return a;
+  if (!(a.h > 0.0f)) return b;
+  if (a.e < b.e) {
+    const FS t = a;
+    a = b;
+    b = t;
+  }
+  const int k = b.e - a.e;  // <= 0
+  if (k < -100) return a;   // below 2^-100 of a: nothing left at pair precision
+  const float sc = __int_as_float((k + 127) << 23);
+  FS r;
+  pair_sum2(a.h, a.l, b.h * sc, b.l * sc, r.h, r.l);
+  r.e = a.e;
+  return r;
+}
+
+__device__ __forceinline__ FS shfl_up_fs(FS v, int o) {
+  FS r;
+  r.h = __shfl_up_sync(0xffffffffu, v.h, o);
+  r.l = __shfl_up_sync(0xffffffffu, v.l, o);
+  r.e = __shfl_up_sync(0xffffffffu, v.e, o);
+  return r;
+}
+
+__device__ __forceinline__ FS shfl_xor_fs(FS v, int o) {
+  FS r;
+  r.h = __shfl_xor_sync(0xffffffffu, v.h, o);
+  r.l = __shfl_xor_sync(0xffffffffu, v.l, o);
+  r.e = __shfl_xor_sync(0xffffffffu, v.e, o);
+  return r;
+}
+
+// natural log of a (> 0) as an fp32 pair, to fp32 accuracy of the mantissa's log
+__device__ __forceinline__ void fs_log_pair(FS a, float &lh, float &ll) {
+  if (!(a.h > 0.0f)) {
+    lh = -INFINITY;
+    ll = 0.0f;
+    return;
+  }
+  const float ln2_hi = 0.693147182464599609375f, ln2_lo = -1.904654323148236017e-9f;
+  const float ef = (float)a.e;
+  const float ph = ef * ln2_hi;
+  const float pe = fmaf(ef, ln2_hi, -ph) + ef * ln2_lo;
+  pair_sum2(ph, pe, logf(a.h) + a.l / a.h, 0.0f, lh, ll);
+}
+
+__device__ __forceinline__ FS fs_from_ss(ScaledSum s) {
+  FS r;
+  if (!(s.q > 0.0)) return fs_zero();
+  pair_of(s.q, r.h, r.l);
+  r.e = s.e;
+  return r;
+}
+
+__device__ __forceinline__ ScaledSum ss_from_fs(FS f) {
+  ScaledSum r;
+  if (!(f.h > 0.0f)) return ss_zero();
+  r.q = (double)f.h + (double)f.l;
+  r.e = f.e;
+  return r;
+}
+
+// log of a pair-scaled value as FP64 (an output)
+__device__ __forceinline__ double fs_log_d(FS a) {
+  if (!(a.h > 0.0f)) return -INFINITY;
+  return (double)(logf(a.h) + a.l / a.h) + (double)a.e * GBNS_LN2;
+}
+
+struct EvScanFsSmem {
+  FS ws[32];
+  FS red[3][32];
+};
+
+// CTA scan of pair-scaled values: inclusive and exclusive prefix of each thread's value, and
+// the total.
+__device__ __forceinline__ void cta_scan_fs(FS v, FS &incl, FS &excl, FS &tot, EvScanFsSmem &sm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const FS u = shfl_up_fs(v, o);
+    if (lane >= o) v = fs_sum(u, v);
+  }
+  const FS wex = shfl_up_fs(v, 1);
+  if (lane == 31) sm.ws[w] = v;
+  __syncthreads();
+  if (w == 0) {
+    FS x = lane < nw ? sm.ws[lane] : fs_zero();
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const FS u = shfl_up_fs(x, o);
+      if (lane >= o) x = fs_sum(u, x);
+    }
+    if (lane < nw) sm.ws[lane] = x;
+  }
+  __syncthreads();
+  const FS pw = w > 0 ? sm.ws[w - 1] : fs_zero();
+  incl = fs_sum(pw, v);
+  excl = lane == 0 ? pw : fs_sum(pw, wex);
+  tot = sm.ws[nw - 1];
+  __syncthreads();
+}
+
 // Process elements [0, M) of log-likelihoods L (fp32) with live-point counts given by
 // nmode: nconst > 0 -> n_k = nconst; ndesc > 0 -> n_k = ndesc - k; else n_k = narr[k].
 // Called by every thread of the CTA (blockDim a multiple of 32).  Optional per-element
@@ -403,8 +500,12 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
                                   double *__restrict__ out_lX, double *__restrict__ out_ldZ,
                                   double *__restrict__ out_lZ, double Loff, const int *__restrict__ Lidx,
                                   EvScanSmem &sm) {
+  __shared__ EvScanFsSmem fsm;
   const int tid = threadIdx.x, T = blockDim.x;
-  ScaledSum pZ = ss_zero(), pZ2 = ss_zero(), pdZ2 = ss_zero();  // this thread's partial sums
+  FS pZ = fs_zero(), pZ2 = fs_zero(), pdZ2 = fs_zero();  // this thread's partial sums
+  float off_h, off_l;
+  pair_of(Loff, off_h, off_l);
+  const float ln2_h = 0.693147182464599609375f, ln2_l = -1.904654323148236017e-9f;
   for (long long base = 0; base < M; base += T) {
     const long long k = base + tid;
     const bool valid = k < M;
@@ -425,38 +526,65 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
     cta_scan_d2(sT, sT2, totT, totT2, sm);
     const double lX_prev = acc.lX + (sT - lT), lX2_prev = acc.lX2 + (sT2 - lT2);
     const double lX_cur = acc.lX + sT;
-    const double lmid = valid ? log_midpoint(Lk, Lm1) + Loff : -INFINITY;
-    const double v_dZ = valid ? (lX_prev + lt) + lmid : -INFINITY;
-    const double v_c = valid ? ((lX2_prev + ltT) + lmid) - lX_cur : -INFINITY;
-    const double v_t2 = valid ? (lX2_prev + lt2) + 2.0 * lmid : -INFINITY;
+    // log((L_k + L_{k-1}) / 2) as an fp32 pair relative to nothing: max + log1p(exp(-|d|)) - ln 2
+    // + Loff; -inf when the element is outside the chunk
+    float mh = -INFINITY, ml = 0.0f;
+    if (valid) {
+      const float m = fmaxf(Lk, Lm1), d = Lk - Lm1;
+      if (isnan(d)) {
+        mh = Lk + Lm1;  // both -inf (or +inf)
+      } else {
+        float th, tl;
+        pair_sum2(m, 0.0f, log1pf(__expf(-fabsf(d))), 0.0f, th, tl);
+        pair_sum2(th, tl, -ln2_h, -ln2_l, th, tl);
+        pair_sum2(th, tl, off_h, off_l, mh, ml);
+      }
+    }
+    // v_dZ = (lX_prev + lt) + lmid, v_c = ((lX2_prev + ltT) - lX_cur) + lmid,
+    // v_t2 = (lX2_prev + lt2) + 2 lmid: the FP64 parts as pairs, then pair sums
+    float ah, al, bh, bl, ch, cl;
+    pair_of(lX_prev + lt, ah, al);
+    pair_of((lX2_prev + ltT) - lX_cur, bh, bl);
+    pair_of(lX2_prev + lt2, ch, cl);
+    float dzh = -INFINITY, dzl = 0.0f, vch = -INFINITY, vcl = 0.0f, t2h = -INFINITY, t2l = 0.0f;
+    if (valid && mh > -INFINITY) {
+      pair_sum2(ah, al, mh, ml, dzh, dzl);
+      pair_sum2(bh, bl, mh, ml, vch, vcl);
+      pair_sum2(ch, cl, 2.0f * mh, 2.0f * ml, t2h, t2l);
+    }
     // A_{k-1} = A_0 + the exclusive prefix of c
-    ScaledSum cin, cex, ctot;
-    cta_scan_ss(ss_term(v_c), cin, cex, ctot, sm);
-    const ScaledSum Ap = ss_sum(acc.A, cex);
-    const double lA_prev = (Ap.q > 0.0) ? (double)logf((float)Ap.q) + (double)Ap.e * GBNS_LN2 : -INFINITY;
-    const double v_t1 = valid ? ((GBNS_LN2 + lX_prev + lt) + lmid) + lA_prev : -INFINITY;
+    FS cin, cex, ctot;
+    cta_scan_fs(fs_term(vch, vcl), cin, cex, ctot, fsm);
+    const FS Ap = fs_sum(fs_from_ss(acc.A), cex);
+    float lah, lal;
+    fs_log_pair(Ap, lah, lal);
+    float t1h = -INFINITY, t1l = 0.0f;
+    if (valid && dzh > -INFINITY && lah > -INFINITY) {
+      pair_sum2(dzh, dzl, ln2_h, ln2_l, t1h, t1l);
+      pair_sum2(t1h, t1l, lah, lal, t1h, t1l);
+    }
     if (valid) {
       if (out_lX) out_lX[k] = lX_cur;
-      if (out_ldZ) out_ldZ[k] = v_dZ;
+      if (out_ldZ) out_ldZ[k] = dzh > -INFINITY ? (double)dzh + (double)dzl : -INFINITY;
     }
-    const ScaledSum tdZ = ss_term(v_dZ), tt2 = ss_term(v_t2);
+    const FS tdZ = fs_term(dzh, dzl), tt2 = fs_term(t2h, t2l);
     if (OUT_LZ) {
-      ScaledSum zin, zex, ztot;
-      cta_scan_ss(tdZ, zin, zex, ztot, sm);
-      if (valid && out_lZ) out_lZ[k] = ss_log(ss_sum(acc.Z, zin));
-      acc.Z = ss_sum(acc.Z, ztot);
+      FS zin, zex, ztot;
+      cta_scan_fs(tdZ, zin, zex, ztot, fsm);
+      if (valid && out_lZ) out_lZ[k] = fs_log_d(fs_sum(fs_from_ss(acc.Z), zin));
+      acc.Z = ss_sum(acc.Z, ss_from_fs(ztot));
     } else {
-      pZ = ss_sum(pZ, tdZ);
+      pZ = fs_sum(pZ, tdZ);
     }
-    pZ2 = ss_sum(pZ2, ss_sum(ss_term(v_t1), tt2));
-    pdZ2 = ss_sum(pdZ2, tt2);
+    pZ2 = fs_sum(pZ2, fs_sum(fs_term(t1h, t1l), tt2));
+    pdZ2 = fs_sum(pdZ2, tt2);
     // carries into the next chunk (the same on every thread)
     const long long last = (M - base < T ? M - base : T) - 1;
     acc.lX += totT;
     acc.lX2 += totT2;
-    acc.A = ss_sum(acc.A, ctot);
+    acc.A = ss_sum(acc.A, ss_from_fs(ctot));
     if (tid == last) {
-      sm.last_ldZ = v_dZ;
+      sm.last_ldZ = dzh > -INFINITY ? (double)dzh + (double)dzl : -INFINITY;
       sm.last_L = Lk;
     }
     __syncthreads();
@@ -464,30 +592,30 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
     acc.Lprev = sm.last_L;
     __syncthreads();
   }
-  // CTA reduction of the partial sums (butterfly in each warp, then across warps)
+  // CTA reduction of the partial sums (butterfly in each warp, then across warps in order)
   const int lane = tid & 31, w = tid >> 5, nw = T >> 5;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    pZ = ss_sum(pZ, shfl_xor_ss(pZ, o));
-    pZ2 = ss_sum(pZ2, shfl_xor_ss(pZ2, o));
-    pdZ2 = ss_sum(pdZ2, shfl_xor_ss(pdZ2, o));
+    pZ = fs_sum(pZ, shfl_xor_fs(pZ, o));
+    pZ2 = fs_sum(pZ2, shfl_xor_fs(pZ2, o));
+    pdZ2 = fs_sum(pdZ2, shfl_xor_fs(pdZ2, o));
   }
   if (lane == 0) {
-    sm.red[0][w] = pZ;
-    sm.red[1][w] = pZ2;
-    sm.red[2][w] = pdZ2;
+    fsm.red[0][w] = pZ;
+    fsm.red[1][w] = pZ2;
+    fsm.red[2][w] = pdZ2;
   }
   __syncthreads();
-  ScaledSum rZ = ss_zero(), rZ2 = ss_zero(), rdZ2 = ss_zero();
+  FS rZ = fs_zero(), rZ2 = fs_zero(), rdZ2 = fs_zero();
   for (int q = 0; q < nw; ++q) {
-    rZ = ss_sum(rZ, sm.red[0][q]);
-    rZ2 = ss_sum(rZ2, sm.red[1][q]);
-    rdZ2 = ss_sum(rdZ2, sm.red[2][q]);
+    rZ = fs_sum(rZ, fsm.red[0][q]);
+    rZ2 = fs_sum(rZ2, fsm.red[1][q]);
+    rdZ2 = fs_sum(rdZ2, fsm.red[2][q]);
   }
   __syncthreads();
-  acc.Z = ss_sum(acc.Z, rZ);
-  acc.Z2 = ss_sum(acc.Z2, rZ2);
-  acc.dZ2 = ss_sum(acc.dZ2, rdZ2);
+  acc.Z = ss_sum(acc.Z, ss_from_fs(rZ));
+  acc.Z2 = ss_sum(acc.Z2, ss_from_fs(rZ2));
+  acc.dZ2 = ss_sum(acc.dZ2, ss_from_fs(rdZ2));
 }
 
 // ------------------------------------------------------------- likelihood ----

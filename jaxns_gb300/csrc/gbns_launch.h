@@ -6,7 +6,15 @@
 namespace gbns {
 
 // Lock-step chain flags of the linear-Gaussian sampler (gbns_lg_bufs.flags).
-enum : int { LG_START = 1, LG_NEED_DIR = 2, LG_PENDING = 4, LG_FAILED = 8, LG_DONE = 16 };
+enum : int {
+  LG_START = 1,
+  LG_NEED_DIR = 2,
+  LG_PENDING = 4,
+  LG_FAILED = 8,
+  LG_DONE = 16,
+  LG_WAIT_REFLECT = 32,  // gradient_guided: reflect the direction at the accepted point first
+  LG_HAVE_GRAD = 64      // the gradient launch has written the chain's gradient at its point
+};
 
 cudaError_t launch_slice_shells(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
 cudaError_t launch_slice_warp(const gbns_batch &b, const float *Lstar, const uint32_t *keys, cudaStream_t stream);
@@ -21,6 +29,7 @@ cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream);
 cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
+cudaError_t launch_lg_chain_step(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t stream);
 cudaError_t lg_tc_prepare(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);
 cudaError_t launch_lg_shell_fused(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t stream);

@@ -133,9 +133,16 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
       }
       ++j;
       flags |= LG_START;
+      // gradient_guided (uni_slice_sampler.py:255-272): the gradient at the accepted point
+      // counts as one evaluation, also after the last slice
+      if (b.gradient_guided) ++total;
       if (j < S) {
-        flags |= LG_NEED_DIR;
-        dir_key = after_key;
+        if (b.gradient_guided) {
+          flags |= LG_WAIT_REFLECT;
+        } else {
+          flags |= LG_NEED_DIR;
+          dir_key = after_key;
+        }
       } else {
         flags |= LG_DONE;
       }
@@ -143,6 +150,22 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
       flags &= ~LG_START;
     }
     flags &= ~LG_PENDING;
+  }
+  // Gradient options: a chain that needs the U-space gradient at its point (after an accepted
+  // point with gradient_guided, at a slice start with gradient_slice) lists itself and sits out
+  // this step; the gradient launch that follows fills lg.grad and sets LG_HAVE_GRAD.
+  bool park = false;
+  float ga = 0.0f, gb = 0.0f;
+  if (!(flags & LG_DONE) && (b.gradient_guided || b.gradient_slice)) {
+    const bool want = (flags & LG_WAIT_REFLECT) || ((flags & LG_START) && b.gradient_slice);
+    if (want && !(flags & LG_HAVE_GRAD)) {
+      park = true;
+      if (lane == 0) lg.grad_list[atomicAdd(lg.grad_count, 1)] = g;
+    } else if (flags & LG_HAVE_GRAD) {
+      const float *gr = lg.grad + (rd.newU_off >> 1) + (size_t)c * P;
+      ga = ha ? gr[pa_] : 0.0f;
+      gb = hb ? gr[pb_] : 0.0f;
+    }
   }
   if (flags & LG_DONE) {
     double *nu = (double *)(b.new_U + rd.newU_off) + (size_t)c * P;
@@ -154,7 +177,26 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
       if (flags & LG_FAILED) atomicOr(&st.status, (int)GBNS_ERR_SHRINK_BUDGET);
       atomicSub(&lg.chains_left[r], 1);
     }
-  } else {
+  } else if (!park) {
+    if (flags & LG_WAIT_REFLECT) {
+      // Householder reflection about the normalised gradient (uni_slice_sampler.py:255-269);
+      // a random direction from split(after_key)[0] when the gradient vanishes or is not finite
+      const float gn = sqrtf(warp_sum(fmaf(ga, ga, gb * gb)));
+      if (!(gn >= 1e-10f) || isinf(gn)) {
+        flags |= LG_NEED_DIR;
+        dir_key = fold(after_key, 0u);
+      } else {
+        const float na = ga / gn, nb = gb / gn;
+        const float dot = warp_sum(fmaf(da, na, db * nb));
+        da = fmaf(-2.0f * dot, na, da);
+        db = fmaf(-2.0f * dot, nb, db);
+        const float dn = sqrtf(warp_sum(fmaf(da, da, db * db)));
+        da = da / dn;
+        db = db / dn;
+        d_changed = true;
+      }
+      flags &= ~LG_WAIT_REFLECT;
+    }
     if (flags & LG_NEED_DIR) {
       if (P == 1) {
         da = 1.0f;
@@ -175,6 +217,19 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
     if (start) {
       after_key = fold(B, 3u);
       alpha = lg_alpha(j, S);
+      bool climb = false;
+      if (b.gradient_slice) {
+        // gradient_slice (uni_slice_sampler.py:202-214): slice along the normalised U-space
+        // gradient at the seed point (t >= 0) unless it vanishes or is not finite; one evaluation
+        ++total;
+        const float gn = sqrtf(warp_sum(fmaf(ga, ga, gb * gb)));
+        if (gn != 0.0f && isfinite(gn)) {
+          climb = true;
+          da = ga / gn;
+          db = gb / gn;
+          d_changed = true;
+        }
+      }
       // chord of u0 + t d in the unit cube; 1 - u = (1 - a) - b keeps the tails exact
       float t1r = INFINITY, t1l = -INFINITY, t0r = INFINITY, t0l = -INFINITY;
 #pragma unroll
@@ -197,7 +252,7 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
         t0l = fmaxf(t0l, __shfl_xor_sync(0xffffffffu, t0l, o));
       }
       right = fminf(t0r, t1r);
-      left = fmaxf(t0l, t1l);
+      left = climb ? 0.0f : fmaxf(t0l, t1l);
       in_slice = 0;
     } else {
       if (t < 0.f) left = t;
@@ -224,6 +279,7 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
       if (hb) W[pb_] = wb;
     }
     flags |= LG_PENDING;
+    flags &= ~LG_HAVE_GRAD;
     if (lane == 0 && lg.tile_pending) lg.tile_pending[lg.tile_base[r] + (c >> 7)] = 1;
   }
   if (u_changed) {
@@ -257,6 +313,70 @@ __global__ void __launch_bounds__(256) k_lg_step(gbns_batch b, gbns_lg_bufs lg, 
     lg.after_key[2 * g + 1] = after_key.k1;
     lg.dir_key[2 * g] = dir_key.k0;
     lg.dir_key[2 * g + 1] = dir_key.k1;
+  }
+}
+
+// U-space gradient of log L at the point of every chain listed by the chain step (jax.grad of
+// Model.forward through the prior quantile, as for the other families): d log L / dw =
+// Phi^T (y - Phi w) / sigma^2, times dw/du (Uniform: b; Normal: b sqrt(2 pi) exp(z^2 / 2)).
+// One CTA per listed chain, grid-stride over the list: threads over data rows form the
+// residuals and their products with Phi, then a CTA reduction per dimension (fp32).
+template <int PM>
+__global__ void __launch_bounds__(256) k_lg_grad(gbns_batch b, gbns_lg_bufs lg) {
+  __shared__ float w_s[PM], slope_s[PM];
+  __shared__ float red[8][PM];
+  const int count = *lg.grad_count;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int e = blockIdx.x; e < count; e += gridDim.x) {
+    const long long g = lg.grad_list[e];
+    const int r = lg.chain_run ? lg.chain_run[g] : run_of_chain(b, g);
+    const gbns_run_desc &rd = b.runs[r];
+    const int P = rd.D, N = rd.N;
+    const int c = (int)(g - rd.shell_off);
+    const size_t co = (rd.newU_off >> 1) + (size_t)c * P;
+    const float *fp = b.fparams + rd.param_off;
+    const float *Phi = fp, *y = fp + (size_t)N * P;
+    const float sigma = fp[(size_t)N * P + N];
+    if (tid < P) {
+      const int kind = b.prior_kind[rd.prior_off + tid];
+      const float pa = b.prior_a[rd.prior_off + tid], pb = b.prior_b[rd.prior_off + tid];
+      const float ua = lg.u0[co + tid], la = lg.u0_lo[co + tid];
+      w_s[tid] = prior_quantile_pair(kind, pa, pb, ua, la);
+      if (kind == GBNS_PRIOR_UNIFORM) {
+        slope_s[tid] = pb;
+      } else {
+        const float z = ndtri_pair(ua, la);
+        slope_s[tid] = pb * 2.50662827463f * gbns_fm_exp(0.5f * z * z);
+      }
+    }
+    __syncthreads();
+    float acc[PM];
+#pragma unroll
+    for (int q = 0; q < PM; ++q) acc[q] = 0.0f;
+    for (int i = tid; i < N; i += blockDim.x) {
+      const float *row = Phi + (size_t)i * P;
+      float pw = 0.0f;
+#pragma unroll
+      for (int q = 0; q < PM; ++q)
+        if (q < P) pw = fmaf(row[q], w_s[q], pw);
+      const float res = y[i] - pw;
+#pragma unroll
+      for (int q = 0; q < PM; ++q)
+        if (q < P) acc[q] = fmaf(row[q], res, acc[q]);
+    }
+#pragma unroll
+    for (int q = 0; q < PM; ++q) {
+      const float v = warp_sum(acc[q]);
+      if (lane == 0) red[wid][q] = v;
+    }
+    __syncthreads();
+    if (tid < P) {
+      float sum = 0.0f;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += red[w][tid];
+      lg.grad[co + tid] = sum / (sigma * sigma) * slope_s[tid];
+    }
+    if (tid == 0) lg.flags[g] |= LG_HAVE_GRAD;
+    __syncthreads();
   }
 }
 
@@ -418,6 +538,25 @@ cudaError_t launch_lg_step_kernel(const gbns_batch &b, const gbns_lg_bufs &lg, c
   return cudaLaunchKernelEx(&cfg, k_lg_step, b, lg, (long long)lg.total_chains);
 }
 
+// One chain step; with the gradient options, the list of chains that ask for a gradient is
+// reset before it and the gradient launch follows it.
+cudaError_t launch_lg_chain_step(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
+  const bool grads = b.gradient_guided || b.gradient_slice;
+  cudaError_t e = cudaSuccess;
+  if (grads && (e = cudaMemsetAsync(lg.grad_count, 0, sizeof(int), s)) != cudaSuccess) return e;
+  if ((e = launch_lg_step_kernel(b, lg, s)) != cudaSuccess) return e;
+  if (grads && lg.total_chains > 0) {
+    int dev = 0, sms = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    const long long grid = lg.total_chains < 8LL * sms ? lg.total_chains : 8LL * sms;
+    if (lg.pmax <= 32) k_lg_grad<32><<<(unsigned)grid, 256, 0, s>>>(b, lg);
+    else k_lg_grad<64><<<(unsigned)grid, 256, 0, s>>>(b, lg);
+    e = cudaGetLastError();
+  }
+  return e;
+}
+
 cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cudaStream_t s) {
   if (lg.num_items > 0) {
     if (lg.pmax <= 32) k_lg_resid<32><<<lg.num_items, 256, 0, s>>>(b, lg);
@@ -429,7 +568,7 @@ cudaError_t launch_lg_resid_cc(const gbns_batch &b, const gbns_lg_bufs &lg, cuda
 cudaError_t launch_lg_steps(const gbns_batch &b, const gbns_lg_bufs &lg, int steps, cudaStream_t s) {
   if (lg.use_tc) return launch_lg_steps_tc(b, lg, steps, s);
   for (int q = 0; q < steps; ++q) {
-    cudaError_t e = launch_lg_step_kernel(b, lg, s);
+    cudaError_t e = launch_lg_chain_step(b, lg, s);
     if (e == cudaSuccess) e = launch_lg_resid_cc(b, lg, s);
     if (e != cudaSuccess) return e;
   }
@@ -472,6 +611,8 @@ int lg_check(const gbns_batch *batch, const gbns_lg_bufs *lg) {
                      lg->num_items_tc < 0 || lg->num_ctas_tc < 0 || (lg->num_items_tc > 0 && !lg->items_tc) ||
                      !lg->tile_base || !lg->tile_pending || !lg->tc_done || lg->num_tiles < 0))
     return lg_fail(-1, "gbns_lg: use_tc needs W_hi, W_lo, Phi_hi, Phi_lo, row_base, items_tc and num_ctas_tc >= 0");
+  if ((batch->gradient_guided || batch->gradient_slice) && (!lg->grad || !lg->grad_list || !lg->grad_count))
+    return lg_fail(-1, "gbns_lg: the gradient options need grad, grad_list and grad_count");
   return 0;
 }
 }  // namespace
@@ -500,7 +641,7 @@ int gbns_lg_steps(const gbns_batch *batch, const gbns_lg_bufs *lg, int num_steps
 int gbns_lg_chain_step(const gbns_batch *batch, const gbns_lg_bufs *lg, void *stream) {
   int rc = lg_check(batch, lg);
   if (rc) return rc;
-  cudaError_t e = gbns::launch_lg_step_kernel(*batch, *lg, (cudaStream_t)stream);
+  cudaError_t e = gbns::launch_lg_chain_step(*batch, *lg, (cudaStream_t)stream);
   if (e != cudaSuccess) return lg_fail(-2, cudaGetErrorString(e));
   return 0;
 }

@@ -1119,7 +1119,7 @@ cudaError_t launch_lg_steps_tc(const gbns_batch &b, const gbns_lg_bufs &lg, int 
   if (grid > lg.num_items_tc) grid = lg.num_items_tc;
   const int launches = steps < 0 ? 1 : steps;
   for (int q = 0; q < launches; ++q) {
-    if (steps >= 0 && (e = launch_lg_step_kernel(b, lg, s)) != cudaSuccess) return e;
+    if (steps >= 0 && (e = launch_lg_chain_step(b, lg, s)) != cudaSuccess) return e;
     if (grid > 0) {
       // programmatic serialisation: the prologue (barriers, tensor memory) overlaps the chain
       // step's tail; the kernel waits for that grid before reading its output
@@ -1252,6 +1252,11 @@ int fused_check(const gbns_batch *batch, const gbns_lg_bufs *lg, const char *who
       lg->max_steps < 1) {
     std::snprintf(msg, sizeof msg, "%s: cluster_size must be 8 or 16, rows_per_cta 128, 256 or 512 with "
                   "rows_per_cta * ceil(pmax / 32) <= 512, max_steps >= 1", who);
+    return tc_fail(-1, msg);
+  }
+  if (batch->gradient_guided || batch->gradient_slice) {
+    std::snprintf(msg, sizeof msg, "%s: the gradient options run on the lock step (gbns_lg_steps), not the fused shell",
+                  who);
     return tc_fail(-1, msg);
   }
   return 0;

@@ -185,9 +185,6 @@ class NSBatch:
         if len(gg) > 1:
             raise ValueError("the runs of a batch share the slice sampler's gradient options")
         self.gradient_guided, self.gradient_slice = gg.pop()
-        if (self.gradient_guided or self.gradient_slice) and any(s.family == FAMILY_LINGAUSS for s in specs):
-            raise NotImplementedError("the gradient options of the slice sampler are not on the linear-Gaussian "
-                                      "lock step")
         for r, s in enumerate(specs):
             validate_spec(s, r)
         live_off = np.concatenate([[0], np.cumsum(ns)[:-1]])
@@ -333,9 +330,14 @@ class NSBatch:
         self.kernel_launches = 0
         self._kernels_per_iter = 1 + int(np.count_nonzero(be > bb))
         # linear-Gaussian shells: one fused launch per shell when every run's share of Phi fits in
-        # the shared memory of its cluster (lg_fused=None: whenever it fits)
+        # the shared memory of its cluster (lg_fused=None: whenever it fits); the slice sampler's
+        # gradient options run on the lock step
         self.lg_fused = False
-        if self.lg and self.lg_tc and lg_fused is not False:
+        grads = self.gradient_guided or self.gradient_slice
+        if lg_fused and grads:
+            raise ValueError("the gradient options of the slice sampler run on the linear-Gaussian lock step, "
+                             "not the fused shell")
+        if self.lg and self.lg_tc and lg_fused is not False and not grads:
             for cs in (16, 8):
                 plan = fused_plan([s.N for s in specs], int(self._lgb.pmax), (cs,))
                 if plan is not None:
@@ -363,7 +365,8 @@ class NSBatch:
                          flags=z(nc, torch.int32), left=z(nc), right=z(nc), t=z(nc), alpha=z(nc), logL0=z(nc),
                          ck=z(2 * nc, torch.int32), after_key=z(2 * nc, torch.int32),
                          slices_key=z(2 * nc, torch.int32), dir_key=z(2 * nc, torch.int32), u0=z(nd), u0_lo=z(nd),
-                         dir=z(nd), W=z(nd), ss=z(nc, f64), chains_left=z(len(specs), torch.int32))
+                         dir=z(nd), W=z(nd), ss=z(nc, f64), chains_left=z(len(specs), torch.int32),
+                         grad=z(nd), grad_list=z(nc, torch.int64), grad_count=z(1, torch.int32))
         items = []
         for r, s in enumerate(specs):
             for c0 in range(0, s.shell_size, 64):

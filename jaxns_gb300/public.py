@@ -144,9 +144,6 @@ class UniDimSliceSampler:
         if not self.perfect:
             raise ValueError("Only perfect slice sampler is implemented.")
         self.gradient_slice = bool(self.gradient_slice)
-        if (self.gradient_slice or self.gradient_guided) and self.model.family not in (0, 1):
-            raise NotImplementedError("the gradient options of the slice sampler need the correlated-Gaussian or "
-                                      "Gaussian-shells likelihood (analytic U-space gradients)")
 
     def num_phantom(self) -> int:
         return self.num_phantom_save

@@ -311,12 +311,12 @@ def slice_shell(model, key, L_star, live_U, live_logL, num_chains, num_slices, n
 
 
 def slice_shell_margin(model, key, L_star, live_U, live_logL, num_chains, num_slices, num_phantom=0,
-                       midpoint_shrink=True):
+                       midpoint_shrink=True, gradient_guided=False, gradient_slice=False):
     """slice_shell with, per chain, the smallest |log L - L*| over its accept tests (FP64)."""
     D = model.D
     live_U = np.ascontiguousarray(live_U, np.float64)
     live_logL = np.ascontiguousarray(live_logL, np.float64)
-    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), 0, 0)
+    cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided), int(gradient_slice))
     U = np.zeros((num_chains, D))
     L = np.zeros(num_chains)
     E = np.zeros(num_chains, np.int64)

@@ -327,3 +327,67 @@ def test_fused_shell_matches_lock_step(gpu_lib):
         o = int(fused.offsets["shell"][r])
         ok = same[o:o + specs[r].shell_size]
         np.testing.assert_allclose(U1[ok], U2[ok], rtol=0, atol=1e-5)
+
+
+@pytest.mark.parametrize("guided,climb,S", [(True, False, 3), (False, True, 3), (True, True, 2)])
+def test_lingauss_gradient_options_chain_parity(gpu_lib, oracle_mod, guided, climb, S):
+    """UniDimSliceSampler's gradient options on the linear-Gaussian lock step: gradient_guided
+    (Householder reflection of the direction about the U-space gradient at each accepted point,
+    uni_slice_sampler.py:255-272) and gradient_slice (each slice along the normalised gradient
+    at its seed, t >= 0, :202-214), one evaluation per gradient.  The device gradient is
+    Phi^T (y - Phi w) / sigma^2 times dw/du in fp32; each direction then carries fp32-vs-FP64
+    differences into the next slice, so the comparison with the FP64 oracle covers a few slices:
+    every chain that stayed clear of the contour by ten times the lock step's rounding band
+    matches, and at least 90 % of all chains do."""
+    import ctypes
+    import jaxns_gb300 as gb
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.engine import NSBatch
+    Phi, y = blr(500, 6, seed=4)
+    model = blr_model(gb, Phi, y)
+    n = 100
+    ns = gb.NestedSampler(model, num_live_points=n, num_slices=S)
+    spec = ns.nested_sampler.run_spec(gb.random.PRNGKey(9), ns.normalise_term_cond(None))
+    spec.gradient_guided, spec.gradient_slice = guided, climb
+    b = NSBatch([spec])
+    assert not b.lg_fused
+    b.init()
+    live = b.live_view(0)
+    K0 = np.array(b.state()[0]["key"], np.uint32)
+    sample_key = gb.random.split(gb.random.split(K0)[0])[1]
+    s = n // 2
+    Lstar = float(live["log_L"][s - 1].item())
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _ffi.call("gbns_lg_shell_begin", ctypes.byref(b._b), ctypes.byref(b._lgb), stream)
+    for _ in range(400):
+        _ffi.call("gbns_lg_steps", ctypes.byref(b._b), ctypes.byref(b._lgb), 16, stream)
+        if int(b.lg_t["chains_left"][0].item()) == 0:
+            break
+    torch.cuda.synchronize()
+    assert int(b.state()[0]["status"]) == 0
+    E_g = b.new_E[:s].cpu().numpy()
+    assert np.all(E_g >= S * (1 + int(guided) + int(climb)))  # a proposal and each gradient per slice
+    om = oracle_mod.lingauss_model(Phi, y, 0.5, 1.0)
+    U_o, L_o, E_o, M_o = oracle_mod.slice_shell_margin(om, sample_key, Lstar, live["U"].cpu().double().numpy(),
+                                                       live["log_L"].cpu().double().numpy(), s, S,
+                                                       gradient_guided=guided, gradient_slice=climb)
+    U_g = b.new_U_view(0).cpu().numpy()
+    same = (E_g == E_o) & np.all(np.abs(U_g - U_o) < 2e-4, axis=1)
+    band = 10 * (1e-3 + 1e-5 * abs(Lstar))
+    bad = np.nonzero((M_o > band) & ~same)[0]
+    assert len(bad) == 0, (bad[:5], M_o[bad[:5]], E_g[bad[:5]], E_o[bad[:5]])
+    assert same.mean() >= 0.9, same.mean()
+
+
+def test_lingauss_gradient_guided_evidence(gpu_lib):
+    """NestedSampler(gradient_guided=True) on a Bayesian linear regression end to end (lock step
+    with the gradient launch): log Z within 4 sigma of the analytic value."""
+    import jaxns_gb300 as gb
+    from jaxns_gb300.adjoint import blr_log_evidence
+    Phi, y = blr(1024, 8, seed=5)
+    model = blr_model(gb, Phi, y)
+    ns = gb.NestedSampler(model, num_live_points=200, num_slices=40, gradient_guided=True)
+    reason, state = ns(gb.random.PRNGKey(1), gb.TerminationCondition(dlogZ=1e-4))
+    res = ns.to_results(reason, state)
+    truth, _ = blr_log_evidence(Phi, y, 0.0, np.log(0.5))
+    assert abs(res.log_Z_mean - truth) < 4 * res.log_Z_uncert + 0.05, (res.log_Z_mean, res.log_Z_uncert, truth)

@@ -81,8 +81,8 @@ def test_slice_sampler_validation(kw, exc):
 
 
 def test_slice_sampler_gradient_options():
-    """gradient_slice and gradient_guided reach the run spec (both kernels take them); the
-    linear-Gaussian family has no analytic U-space gradient on the device and refuses them."""
+    """gradient_slice and gradient_guided reach the run spec for every family (the
+    linear-Gaussian family takes them on its lock step)."""
     import jaxns_gb300 as gb
     from jaxns_gb300.public import ShardedStaticNestedSampler, UniDimSliceSampler
     m = _model(2)
@@ -99,9 +99,12 @@ def test_slice_sampler_gradient_options():
         return w
 
     lg = gb.Model(prior_model, gb.LinearGaussianLikelihood(Phi, np.ones(4), 0.5))
-    with pytest.raises(NotImplementedError):
-        UniDimSliceSampler(model=lg, num_slices=5, num_phantom_save=0, midpoint_shrink=True, perfect=True,
-                           gradient_guided=True)
+    smp = UniDimSliceSampler(model=lg, num_slices=5, num_phantom_save=0, midpoint_shrink=True, perfect=True,
+                             gradient_guided=True)
+    ns = ShardedStaticNestedSampler(model=lg, max_samples=1000, init_efficiency_threshold=0.1, sampler=smp,
+                                    num_live_points=20)
+    spec = ns.run_spec(gb.random.PRNGKey(0), gb.TerminationCondition())
+    assert spec.gradient_guided and not spec.gradient_slice and spec.family == 2
 
 
 def test_static_sampler_rounding():
