@@ -509,6 +509,7 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
   for (long long base = 0; base < M; base += T) {
     const long long k = base + tid;
     const bool valid = k < M;
+    const FS A0 = fs_from_ss(acc.A), Z0 = OUT_LZ ? fs_from_ss(acc.Z) : fs_zero();  // the chunk's carries
     const float Lk = valid ? L[Lidx ? Lidx[k] : k] : 0.0f;
     const float Lm1 = !valid ? 0.0f : (k == 0 ? acc.Lprev : L[Lidx ? Lidx[k - 1] : k - 1]);
     int nk = 1;
@@ -555,7 +556,7 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
     // A_{k-1} = A_0 + the exclusive prefix of c
     FS cin, cex, ctot;
     cta_scan_fs(fs_term(vch, vcl), cin, cex, ctot, fsm);
-    const FS Ap = fs_sum(fs_from_ss(acc.A), cex);
+    const FS Ap = fs_sum(A0, cex);
     float lah, lal;
     fs_log_pair(Ap, lah, lal);
     float t1h = -INFINITY, t1l = 0.0f;
@@ -571,7 +572,7 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
     if (OUT_LZ) {
       FS zin, zex, ztot;
       cta_scan_fs(tdZ, zin, zex, ztot, fsm);
-      if (valid && out_lZ) out_lZ[k] = fs_log_d(fs_sum(fs_from_ss(acc.Z), zin));
+      if (valid && out_lZ) out_lZ[k] = fs_log_d(fs_sum(Z0, zin));
       acc.Z = ss_sum(acc.Z, ss_from_fs(ztot));
     } else {
       pZ = fs_sum(pZ, tdZ);

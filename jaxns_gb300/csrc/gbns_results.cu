@@ -345,16 +345,10 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
     }
   }
   __syncthreads();
-  // normalise_log_space(log_dZ_mean) and H (sharded_static.py:726-737)
-  float mx = -INFINITY;
-  for (long long i = threadIdx.x; i < N; i += blockDim.x) mx = fmaxf(mx, (float)ldp[i]);
-  mx = cta_max_f(mx, (float *)dred);
-  double se = 0.0;
-  if (mx > -INFINITY)
-    for (long long i = threadIdx.x; i < N; i += blockDim.x) se += (double)__expf((float)(ldp[i] - (double)mx));
-  se = cta_sum_d(se, dred);
-  const double norm = (mx > -INFINITY) ? (double)mx + log(se) : -INFINITY;
+  // normalise_log_space(log_dZ_mean) and H (sharded_static.py:726-737): the normaliser
+  // logsumexp(log_dZ_mean) is log sum dZ = log Z, which the scan has just accumulated
   const double lZ = s_lz[0], lZ2 = s_lz[1], ldZ2 = s_lz[2];
+  const double norm = lZ;
   const double mu = 2.0 * lZ - 0.5 * lZ2;
   double h1 = 0.0, h2 = 0.0;
   for (long long i = threadIdx.x; i < N; i += blockDim.x) {
