@@ -47,6 +47,16 @@ extern "C" {
 
 #define GBNS_VERSION 1
 
+/* Rows of the shrinkage-coefficient table (gbns_batch.ncoef, gbns_evidence_stats): row n holds
+ * the n-only terms of _update_evidence_calc_op (internals/shrinkage_statistics.py:55-73) for
+ * n live points,
+ *   doubles 0-4   FP64 log T = -log1p(1/n), log t = -log(n+1), log T2 = -log1p(2/n),
+ *                 log t2 = log 2 - log(n+1) - log(n+2), log tT = -log1p(1/n) - log(n+2);
+ *   bytes 64-103  the same five as fp32 pairs (hi, lo), hi = fl32(v), lo = fl32(v - hi)
+ *                 (lo = 0 where hi is infinite);
+ * the rest of the row is unused.  The table must be 16-byte aligned. */
+#define GBNS_NCOEF_STRIDE 16
+
 /* likelihood families (a fused CUDA likelihood cannot be an arbitrary Python callable) */
 enum gbns_family {
     GBNS_LIK_MVN = 0,      /* log N(x; mu, L L^T), L lower Cholesky (params: mu, Linv, c0) */
@@ -165,7 +175,8 @@ typedef struct {
     const int *prior_kind;          /* [sum D] */
     const float *prior_a;           /* [sum D] */
     const float *prior_b;           /* [sum D] */
-    const double *ncoef;            /* [(ncoef_n+1) * 8] FP64 shrinkage coefficients per count */
+    const double *ncoef;            /* [(ncoef_n+1) * GBNS_NCOEF_STRIDE] shrinkage coefficients per count
+                                       (layout at GBNS_NCOEF_STRIDE) */
     const int *items;               /* [num_items * 4] (run, chain_begin, chain_count, 0) */
     int num_items;
     int bucket_begin[8];            /* work-item ranges per dimension bucket */
@@ -364,6 +375,8 @@ int gbns_evidence_adjoint_tc(const double *U_dev, const double *log_w_dev, long 
  * counts and log-likelihoods (FP64), M < 2^32; log_Z_dev: [S]. */
 int gbns_sample_evidence(const uint32_t *key_dev, const int *num_live_dev, const double *log_L_dev, long long M,
                          int S, double *log_Z_dev, void *stream);
+/* compute_evidence_stats over one sorted sample set: ncoef_dev is a coefficient table of nmax + 1
+ * rows (GBNS_NCOEF_STRIDE) */
 int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,
                         int nmax, gbns_evcalc *final_dev, double *log_X_mean_dev, double *log_dZ_mean_dev,
                         double *log_Z_mean_dev, void *stream);

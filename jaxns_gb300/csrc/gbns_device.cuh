@@ -239,51 +239,11 @@ __device__ __forceinline__ ScaledSum ss_sum(ScaledSum a, ScaledSum b) {
 }
 
 struct EvScanSmem {
-  double wa[32], wb[32];
+  double carry_lX, fin_lX, fin_lX2;
+  ScaledSum fin[4];  // A, Z, Z2, dZ2 after the scan
   double last_ldZ;
   float last_L;
 };
-
-// Inclusive CTA scan of two FP64 sums; every thread also gets the CTA totals.
-__device__ __forceinline__ void cta_scan_d2(double &a, double &b, double &ta, double &tb, EvScanSmem &sm) {
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const double a2 = __shfl_up_sync(0xffffffffu, a, o), b2 = __shfl_up_sync(0xffffffffu, b, o);
-    if (lane >= o) {
-      a += a2;
-      b += b2;
-    }
-  }
-  if (lane == 31) {
-    sm.wa[w] = a;
-    sm.wb[w] = b;
-  }
-  __syncthreads();
-  if (w == 0) {
-    double x = lane < nw ? sm.wa[lane] : 0.0, y = lane < nw ? sm.wb[lane] : 0.0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const double x2 = __shfl_up_sync(0xffffffffu, x, o), y2 = __shfl_up_sync(0xffffffffu, y, o);
-      if (lane >= o) {
-        x += x2;
-        y += y2;
-      }
-    }
-    if (lane < nw) {
-      sm.wa[lane] = x;
-      sm.wb[lane] = y;
-    }
-  }
-  __syncthreads();
-  if (w > 0) {
-    a += sm.wa[w - 1];
-    b += sm.wb[w - 1];
-  }
-  ta = sm.wa[nw - 1];
-  tb = sm.wb[nw - 1];
-  __syncthreads();
-}
 
 struct EvAcc {
   double lX, lX2;
@@ -489,11 +449,56 @@ __device__ __forceinline__ void cta_scan_fs(FS v, FS &incl, FS &excl, FS &tot, E
   __syncthreads();
 }
 
+struct EvScanPairSmem {
+  float4 w[32];
+};
+
+// Inclusive CTA scan of two fp32 pairs (a = ah + al, b = bh + bl); every thread also gets
+// the CTA totals.
+__device__ __forceinline__ void cta_scan_p2(float &ah, float &al, float &bh, float &bl, float4 &tot,
+                                            EvScanPairSmem &sm) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const float uah = __shfl_up_sync(0xffffffffu, ah, o), ual = __shfl_up_sync(0xffffffffu, al, o);
+    const float ubh = __shfl_up_sync(0xffffffffu, bh, o), ubl = __shfl_up_sync(0xffffffffu, bl, o);
+    if (lane >= o) {
+      pair_sum2(uah, ual, ah, al, ah, al);
+      pair_sum2(ubh, ubl, bh, bl, bh, bl);
+    }
+  }
+  if (lane == 31) sm.w[w] = make_float4(ah, al, bh, bl);
+  __syncthreads();
+  if (w == 0) {
+    float4 x = lane < nw ? sm.w[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const float uah = __shfl_up_sync(0xffffffffu, x.x, o), ual = __shfl_up_sync(0xffffffffu, x.y, o);
+      const float ubh = __shfl_up_sync(0xffffffffu, x.z, o), ubl = __shfl_up_sync(0xffffffffu, x.w, o);
+      if (lane >= o) {
+        pair_sum2(uah, ual, x.x, x.y, x.x, x.y);
+        pair_sum2(ubh, ubl, x.z, x.w, x.z, x.w);
+      }
+    }
+    if (lane < nw) sm.w[lane] = x;
+  }
+  __syncthreads();
+  if (w > 0) {
+    const float4 p = sm.w[w - 1];
+    pair_sum2(p.x, p.y, ah, al, ah, al);
+    pair_sum2(p.z, p.w, bh, bl, bh, bl);
+  }
+  tot = sm.w[nw - 1];
+  __syncthreads();
+}
+
 // Process elements [0, M) of log-likelihoods L (fp32) with live-point counts given by
 // nmode: nconst > 0 -> n_k = nconst; ndesc > 0 -> n_k = ndesc - k; else n_k = narr[k].
-// Called by every thread of the CTA (blockDim a multiple of 32).  Optional per-element
-// outputs (FP64 logs): log X, log dZ and, with OUT_LZ, the running log Z.  L values are
-// relative to Loff (added back in FP64); Lidx, when given, gathers L[Lidx[k]].
+// Called by every thread of the CTA (blockDim a multiple of 32), each holding the same acc.
+// Optional per-element outputs (FP64 logs): log X, log dZ and, with OUT_LZ, the running log Z.
+// L values are relative to Loff (added back in FP64); Lidx, when given, gathers L[Lidx[k]].
+// Inside the loop every thread carries pair copies of log X, log X2, A and Z; thread 0 alone
+// keeps the FP64 carries (in shared memory), which every thread reads back at the end.
 template <bool OUT_LZ>
 __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long long M, int nconst, int ndesc,
                                   const int *__restrict__ narr, const double *__restrict__ ncoef, int nmax,
@@ -501,34 +506,55 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
                                   double *__restrict__ out_lZ, double Loff, const int *__restrict__ Lidx,
                                   EvScanSmem &sm) {
   __shared__ EvScanFsSmem fsm;
+  __shared__ EvScanPairSmem psm;
   const int tid = threadIdx.x, T = blockDim.x;
   FS pZ = fs_zero(), pZ2 = fs_zero(), pdZ2 = fs_zero();  // this thread's partial sums
   float off_h, off_l;
   pair_of(Loff, off_h, off_l);
   const float ln2_h = 0.693147182464599609375f, ln2_l = -1.904654323148236017e-9f;
+  float lxh, lxl, lx2h, lx2l;  // pair copies of the carried log X, log X2
+  pair_of(acc.lX, lxh, lxl);
+  pair_of(acc.lX2, lx2h, lx2l);
+  FS A0 = fs_from_ss(acc.A), Z0 = fs_from_ss(acc.Z);
+  if (tid == 0) sm.carry_lX = acc.lX;
+  __syncthreads();
   for (long long base = 0; base < M; base += T) {
     const long long k = base + tid;
     const bool valid = k < M;
-    const FS A0 = fs_from_ss(acc.A), Z0 = OUT_LZ ? fs_from_ss(acc.Z) : fs_zero();  // the chunk's carries
     const float Lk = valid ? L[Lidx ? Lidx[k] : k] : 0.0f;
     const float Lm1 = !valid ? 0.0f : (k == 0 ? acc.Lprev : L[Lidx ? Lidx[k - 1] : k - 1]);
     int nk = 1;
     if (valid) nk = nconst > 0 ? nconst : (ndesc > 0 ? (int)(ndesc - k) : narr[k]);
     nk = nk < 0 ? 0 : nk;
-    double cf[5];
+    // the n-only coefficients (T, t, T2, t2, tT) as fp32 pairs: bytes 64-103 of the table row
+    float cp[10];
     if (nk <= nmax) {
-      const double *c = ncoef + (size_t)nk * 8;
-      cf[0] = c[0]; cf[1] = c[1]; cf[2] = c[2]; cf[3] = c[3]; cf[4] = c[4];
+      const float4 *c = (const float4 *)(ncoef + (size_t)nk * GBNS_NCOEF_STRIDE + 8);
+      const float4 c0 = c[0], c1 = c[1];
+      const float2 c2 = *(const float2 *)(c + 2);
+      cp[0] = c0.x; cp[1] = c0.y; cp[2] = c0.z; cp[3] = c0.w;
+      cp[4] = c1.x; cp[5] = c1.y; cp[6] = c1.z; cp[7] = c1.w;
+      cp[8] = c2.x; cp[9] = c2.y;
     } else {
+      double cf[5];
       ncoef_compute((double)nk, cf);
+#pragma unroll
+      for (int q = 0; q < 5; ++q) pair_of(cf[q], cp[2 * q], cp[2 * q + 1]);
     }
-    const double lT = valid ? cf[0] : 0.0, lt = cf[1], lT2 = valid ? cf[2] : 0.0, lt2 = cf[3], ltT = cf[4];
-    double sT = lT, sT2 = lT2, totT, totT2;
-    cta_scan_d2(sT, sT2, totT, totT2, sm);
-    const double lX_prev = acc.lX + (sT - lT), lX2_prev = acc.lX2 + (sT2 - lT2);
-    const double lX_cur = acc.lX + sT;
-    // log((L_k + L_{k-1}) / 2) as an fp32 pair relative to nothing: max + log1p(exp(-|d|)) - ln 2
-    // + Loff; -inf when the element is outside the chunk
+    // log X and log X2 of this element: the carried values plus the CTA's pair prefix of
+    // log T and log T2
+    float sTh = valid ? cp[0] : 0.0f, sTl = valid ? cp[1] : 0.0f;
+    float sT2h = valid ? cp[4] : 0.0f, sT2l = valid ? cp[5] : 0.0f;
+    float4 tot;
+    cta_scan_p2(sTh, sTl, sT2h, sT2l, tot, psm);
+    float xch, xcl, xph, xpl, x2ph, x2pl, eh, el;
+    pair_sum2(lxh, lxl, sTh, sTl, xch, xcl);                          // log X_k
+    pair_sum2(sTh, sTl, valid ? -cp[0] : 0.0f, valid ? -cp[1] : 0.0f, eh, el);
+    pair_sum2(lxh, lxl, eh, el, xph, xpl);                            // log X_{k-1}
+    pair_sum2(sT2h, sT2l, valid ? -cp[4] : 0.0f, valid ? -cp[5] : 0.0f, eh, el);
+    pair_sum2(lx2h, lx2l, eh, el, x2ph, x2pl);                        // log X2_{k-1}
+    // log((L_k + L_{k-1}) / 2) + Loff as a pair: max + log1p(exp(-|d|)) - ln 2 + Loff; -inf
+    // outside the chunk
     float mh = -INFINITY, ml = 0.0f;
     if (valid) {
       const float m = fmaxf(Lk, Lm1), d = Lk - Lm1;
@@ -542,16 +568,17 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
       }
     }
     // v_dZ = (lX_prev + lt) + lmid, v_c = ((lX2_prev + ltT) - lX_cur) + lmid,
-    // v_t2 = (lX2_prev + lt2) + 2 lmid: the FP64 parts as pairs, then pair sums
-    float ah, al, bh, bl, ch, cl;
-    pair_of(lX_prev + lt, ah, al);
-    pair_of((lX2_prev + ltT) - lX_cur, bh, bl);
-    pair_of(lX2_prev + lt2, ch, cl);
+    // v_t2 = (lX2_prev + lt2) + 2 lmid
     float dzh = -INFINITY, dzl = 0.0f, vch = -INFINITY, vcl = 0.0f, t2h = -INFINITY, t2l = 0.0f;
     if (valid && mh > -INFINITY) {
+      float ah, al;
+      pair_sum2(xph, xpl, cp[2], cp[3], ah, al);
       pair_sum2(ah, al, mh, ml, dzh, dzl);
-      pair_sum2(bh, bl, mh, ml, vch, vcl);
-      pair_sum2(ch, cl, 2.0f * mh, 2.0f * ml, t2h, t2l);
+      pair_sum2(x2ph, x2pl, cp[8], cp[9], ah, al);
+      pair_sum2(ah, al, -xch, -xcl, ah, al);
+      pair_sum2(ah, al, mh, ml, vch, vcl);
+      pair_sum2(x2ph, x2pl, cp[6], cp[7], ah, al);
+      pair_sum2(ah, al, 2.0f * mh, 2.0f * ml, t2h, t2l);
     }
     // A_{k-1} = A_0 + the exclusive prefix of c
     FS cin, cex, ctot;
@@ -565,30 +592,38 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
       pair_sum2(t1h, t1l, lah, lal, t1h, t1l);
     }
     if (valid) {
-      if (out_lX) out_lX[k] = lX_cur;
+      if (out_lX) out_lX[k] = sm.carry_lX + ((double)sTh + (double)sTl);
       if (out_ldZ) out_ldZ[k] = dzh > -INFINITY ? (double)dzh + (double)dzl : -INFINITY;
     }
     const FS tdZ = fs_term(dzh, dzl), tt2 = fs_term(t2h, t2l);
+    FS ztot = fs_zero();
     if (OUT_LZ) {
-      FS zin, zex, ztot;
+      FS zin, zex;
       cta_scan_fs(tdZ, zin, zex, ztot, fsm);
       if (valid && out_lZ) out_lZ[k] = fs_log_d(fs_sum(Z0, zin));
-      acc.Z = ss_sum(acc.Z, ss_from_fs(ztot));
+      Z0 = fs_sum(Z0, ztot);
     } else {
       pZ = fs_sum(pZ, tdZ);
     }
     pZ2 = fs_sum(pZ2, fs_sum(fs_term(t1h, t1l), tt2));
     pdZ2 = fs_sum(pdZ2, tt2);
-    // carries into the next chunk (the same on every thread)
+    // carries into the next chunk: pairs in every thread, FP64 in thread 0
+    pair_sum2(lxh, lxl, tot.x, tot.y, lxh, lxl);
+    pair_sum2(lx2h, lx2l, tot.z, tot.w, lx2h, lx2l);
+    A0 = fs_sum(A0, ctot);
     const long long last = (M - base < T ? M - base : T) - 1;
-    acc.lX += totT;
-    acc.lX2 += totT2;
-    acc.A = ss_sum(acc.A, ss_from_fs(ctot));
     if (tid == last) {
       sm.last_ldZ = dzh > -INFINITY ? (double)dzh + (double)dzl : -INFINITY;
       sm.last_L = Lk;
     }
-    __syncthreads();
+    __syncthreads();  // every thread has read sm.carry_lX for this chunk
+    if (tid == 0) {
+      acc.lX += (double)tot.x + (double)tot.y;
+      acc.lX2 += (double)tot.z + (double)tot.w;
+      acc.A = ss_sum(acc.A, ss_from_fs(ctot));
+      if (OUT_LZ) acc.Z = ss_sum(acc.Z, ss_from_fs(ztot));
+      sm.carry_lX = acc.lX;
+    }
     acc.ldZ_last = sm.last_ldZ;
     acc.Lprev = sm.last_L;
     __syncthreads();
@@ -607,16 +642,31 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
     fsm.red[2][w] = pdZ2;
   }
   __syncthreads();
-  FS rZ = fs_zero(), rZ2 = fs_zero(), rdZ2 = fs_zero();
-  for (int q = 0; q < nw; ++q) {
-    rZ = fs_sum(rZ, fsm.red[0][q]);
-    rZ2 = fs_sum(rZ2, fsm.red[1][q]);
-    rdZ2 = fs_sum(rdZ2, fsm.red[2][q]);
+  if (tid == 0) {
+    FS rZ = fs_zero(), rZ2 = fs_zero(), rdZ2 = fs_zero();
+    for (int q = 0; q < nw; ++q) {
+      rZ = fs_sum(rZ, fsm.red[0][q]);
+      rZ2 = fs_sum(rZ2, fsm.red[1][q]);
+      rdZ2 = fs_sum(rdZ2, fsm.red[2][q]);
+    }
+    acc.Z = ss_sum(acc.Z, ss_from_fs(rZ));
+    acc.Z2 = ss_sum(acc.Z2, ss_from_fs(rZ2));
+    acc.dZ2 = ss_sum(acc.dZ2, ss_from_fs(rdZ2));
+    sm.fin_lX = acc.lX;
+    sm.fin_lX2 = acc.lX2;
+    sm.fin[0] = acc.A;
+    sm.fin[1] = acc.Z;
+    sm.fin[2] = acc.Z2;
+    sm.fin[3] = acc.dZ2;
   }
   __syncthreads();
-  acc.Z = ss_sum(acc.Z, ss_from_fs(rZ));
-  acc.Z2 = ss_sum(acc.Z2, ss_from_fs(rZ2));
-  acc.dZ2 = ss_sum(acc.dZ2, ss_from_fs(rdZ2));
+  acc.lX = sm.fin_lX;
+  acc.lX2 = sm.fin_lX2;
+  acc.A = sm.fin[0];
+  acc.Z = sm.fin[1];
+  acc.Z2 = sm.fin[2];
+  acc.dZ2 = sm.fin[3];
+  __syncthreads();
 }
 
 // ------------------------------------------------------------- likelihood ----

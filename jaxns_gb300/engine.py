@@ -67,6 +67,9 @@ class RunSpec:
     gradient_slice: bool = False
 
 
+NCOEF_STRIDE = 16  # doubles per row of the coefficient table
+
+
 def ncoef_table(nmax: int) -> np.ndarray:
     """FP64 shrinkage coefficients per live-point count n (the n-only terms of
     _update_evidence_calc_op, internals/shrinkage_statistics.py:55-73)."""
@@ -80,8 +83,17 @@ def ncoef_table(nmax: int) -> np.ndarray:
         T2 = -np.logaddexp(0.0, np.log(2.0) - lnn)
         t2 = np.log(2.0) - lnn1 - lnn2
         tT = -np.logaddexp(0.0, -lnn) - lnn2
-    out = np.zeros((nmax + 1, 8), np.float64)
-    out[:, 0], out[:, 1], out[:, 2], out[:, 3], out[:, 4] = T, t, T2, t2, tT
+    out = np.zeros((nmax + 1, NCOEF_STRIDE), np.float64)
+    vals = np.stack([T, t, T2, t2, tT], axis=1)
+    out[:, :5] = vals
+    # bytes 64-103 of a row: the same five as fp32 pairs (hi, lo), hi + lo = the FP64 value to
+    # ~2^-48 relative, for the device scans that work in pair arithmetic
+    hi = vals.astype(np.float32)
+    with np.errstate(invalid="ignore"):
+        lo = np.where(np.isfinite(hi), vals - hi.astype(np.float64), 0.0).astype(np.float32)
+    pairs = np.zeros((nmax + 1, 2 * (NCOEF_STRIDE - 8)), np.float32)
+    pairs[:, 0:10:2], pairs[:, 1:10:2] = hi, lo
+    out[:, 8:] = pairs.view(np.float64)
     return out
 
 

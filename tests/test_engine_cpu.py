@@ -164,7 +164,13 @@ def test_shrinkage_coefficient_table():
         return max(a, b) + math.log1p(math.exp(-abs(a - b)))
 
     tab = ncoef_table(300)
-    assert tab.shape == (301, 8)
+    assert tab.shape == (301, 16)
+    # bytes 64-103: the same five as fp32 pairs hi + lo (the device scans' form), to 2^-48
+    pairs = tab[:, 8:].view(np.float32)
+    hi, lo = pairs[:, 0:10:2].astype(np.float64), pairs[:, 1:10:2].astype(np.float64)
+    assert np.all(hi[1:] == tab[1:, :5].astype(np.float32))
+    np.testing.assert_allclose((hi + lo)[1:], tab[1:, :5], rtol=2.0 ** -46, atol=0)
+    assert np.all(pairs[:, 10:] == 0)
     for n in (1, 2, 3, 7, 50, 299, 300):
         ln, ln1, ln2 = math.log(n), math.log(n + 1), math.log(n + 2)
         want = [-lae(0.0, -ln), -ln1, -lae(0.0, math.log(2.0) - ln), math.log(2.0) - ln1 - ln2, -lae(0.0, -ln) - ln2]
