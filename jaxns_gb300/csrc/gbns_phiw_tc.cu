@@ -239,6 +239,32 @@ __device__ void tc_resid_tile(const TcMaps &maps, int a_row, int b_row, int nkb,
 // the unit's row tiles and add it to the chain's FP64 total once per unit.  Copies, MMAs and
 // epilogue of successive row tiles overlap.  Units whose chain tile has no pending proposal
 // are skipped by every role alike (the flags are read-only during the launch).
+// sum_j (y_j - v_j)^2 over the first n (<= 32) of 32 accumulator columns, in four
+// independent FMA chains (j mod 4) so that the reduction does not serialise on FMA latency
+__device__ __forceinline__ float sq_resid32(const float *ys, const float *v, int n) {
+  float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, p3 = 0.0f;
+  if (n >= 32) {
+#pragma unroll
+    for (int j = 0; j < 32; j += 4) {
+      const float r0 = ys[j] - v[j], r1 = ys[j + 1] - v[j + 1], r2 = ys[j + 2] - v[j + 2], r3 = ys[j + 3] - v[j + 3];
+      p0 = fmaf(r0, r0, p0);
+      p1 = fmaf(r1, r1, p1);
+      p2 = fmaf(r2, r2, p2);
+      p3 = fmaf(r3, r3, p3);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 32; j += 4) {
+      const float r0 = ys[j] - v[j], r1 = ys[j + 1] - v[j + 1], r2 = ys[j + 2] - v[j + 2], r3 = ys[j + 3] - v[j + 3];
+      p0 = j < n ? fmaf(r0, r0, p0) : p0;
+      p1 = j + 1 < n ? fmaf(r1, r1, p1) : p1;
+      p2 = j + 2 < n ? fmaf(r2, r2, p2) : p2;
+      p3 = j + 3 < n ? fmaf(r3, r3, p3) : p3;
+    }
+  }
+  return (p0 + p1) + (p2 + p3);
+}
+
 constexpr int SR_ROWS = 128;                       // data rows per tile (accumulator columns)
 constexpr unsigned SR_BOX = 128 * TC_KB * 4;       // one K block of 128 rows: 16 KB
 constexpr int SR_THREADS = 192;
@@ -473,11 +499,7 @@ __global__ void __launch_bounds__(SR_THREADS) k_lg_resid_tc(const __grid_constan
         for (int ch = 0; ch < nch; ++ch) {
           float v[32];
           tc_ld32(taddr + (uint32_t)(ch * 32), v);
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const float rr = ys[ew][ch * 32 + j] - v[j];
-            part = (ch * 32 + j < nrows) ? fmaf(rr, rr, part) : part;
-          }
+          part += sq_resid32(&ys[ew][ch * 32], v, nrows - ch * 32);
         }
         ssum += (double)part;
         tc_fence_before();
@@ -947,13 +969,7 @@ __global__ void __launch_bounds__(512) k_lg_shell_fused(const __grid_constant__ 
         for (int col = cbeg; col < cend; col += 32) {
           float v[32];
           tc_ld32(taddr + (uint32_t)col, v);
-          float p = 0.0f;
-#pragma unroll
-          for (int q = 0; q < 32; ++q) {
-            const float rr = ys[col + q] - v[q];
-            p = (col + q < cend) ? fmaf(rr, rr, p) : p;
-          }
-          lf_pair_acc(part, part_lo, p);
+          lf_pair_acc(part, part_lo, sq_resid32(ys + col, v, cend - col));
         }
       }
     }
