@@ -23,6 +23,14 @@ struct RunSmem {
   int m;                                // live points above the contour
 };
 
+// Per-warp scratch of the direction pass (dynamic shared memory, one per warp of the CTA, so
+// a CTA reserves only what its warps use)
+template <int DMAX>
+struct DirWarp {
+  uint4 key[32];            // (direction key, lane) of each lane that needs a direction
+  float buf[32][DMAX + 1];  // the normals, one row per lane
+};
+
 // jax.grad of Model.forward w.r.t. U at u (analytic): d log L / dx through the prior quantile
 // (Uniform: dx/du = b; Normal: dx/du = b sqrt(2 pi) exp(z^2 / 2)).  MVN: -Linv^T Linv (x - mu);
 // shells: sum_k softmax_k (-z_k / w) (x - c_k) / r_k.
@@ -197,8 +205,8 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
   // warp is done, so new directions can be generated warp-cooperatively.  A chain's arithmetic
   // does not depend on the lane that runs it.
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  __shared__ float dirbuf[4][32][DMAX + 1];
-  __shared__ uint4 dirkey[4][32];  // (direction key, lane) of each lane that needs a direction
+  extern __shared__ __align__(16) unsigned char slice_dyn[];
+  DirWarp<DMAX> &W = reinterpret_cast<DirWarp<DMAX> *>(slice_dyn)[wid];
   const uint32_t dmagic = ((1u << 20) + (uint32_t)D - 1u) / (uint32_t)D;  // p / D = p * dmagic >> 20 for p < 2^14
 
   // --- keys: _collect_shell split (sharded_static.py:248) then split(sample_key, s)[c]
@@ -272,14 +280,14 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
         if (need_dir) d[0] = 1.0f;
       } else {
         if (need_dir)
-          dirkey[wid][__popc(dmask & ((1u << lane) - 1u))] = make_uint4(dir_key.k0, dir_key.k1, (uint32_t)lane, 0u);
+          W.key[__popc(dmask & ((1u << lane) - 1u))] = make_uint4(dir_key.k0, dir_key.k1, (uint32_t)lane, 0u);
         __syncwarp();
         const int cnt = __popc(dmask) * D;
         for (int p = lane; p < cnt; p += 32) {
           const int g = (int)(((uint32_t)p * dmagic) >> 20);
-          const uint4 e = dirkey[wid][g];
+          const uint4 e = W.key[g];
           const uint32_t jj = (uint32_t)(p - g * D);
-          dirbuf[wid][e.z][jj] = normal_from_bits(bits64(Key{e.x, e.y}, jj));
+          W.buf[e.z][jj] = normal_from_bits(bits64(Key{e.x, e.y}, jj));
         }
         __syncwarp();
         if (need_dir) {
@@ -287,7 +295,7 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
 #pragma unroll
           for (int q = 0; q < DMAX; ++q)
             if (q < D) {
-              d[q] = dirbuf[wid][lane][q];
+              d[q] = W.buf[lane][q];
               ss = fmaf(d[q], d[q], ss);
             }
           const float inv = 1.0f / sqrtf(ss);
@@ -432,6 +440,30 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
   }
 }
 
+using SliceKernel = void (*)(gbns_batch, int, const float *, const uint32_t *);
+
+static size_t dir_warp_bytes(int dmax) {
+  switch (dmax) {
+    case 8: return sizeof(DirWarp<8>);
+    case 16: return sizeof(DirWarp<16>);
+    case 32: return sizeof(DirWarp<32>);
+    default: return sizeof(DirWarp<64>);
+  }
+}
+
+// One launch with the direction scratch of each warp in dynamic shared memory; kernels that
+// need more than the default 48 KB get the opt-in first.
+static cudaError_t launch_slice_kernel(SliceKernel k, int dmax, int nblk, int threads, const gbns_batch &b, int ib,
+                                       const float *Lstar, const uint32_t *keys, cudaStream_t stream) {
+  const size_t smem = (size_t)((threads + 31) / 32) * dir_warp_bytes(dmax);
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  k<<<nblk, threads, smem, stream>>>(b, ib, Lstar, keys);
+  return cudaGetLastError();
+}
+
 template <int DMAX>
 static cudaError_t launch_bucket(const gbns_batch &b, int fam, int ib, int ie, const float *Lstar, const uint32_t *keys,
                                  cudaStream_t stream) {
@@ -442,13 +474,15 @@ static cudaError_t launch_bucket(const gbns_batch &b, int fam, int ib, int ie, c
   if (fam == GBNS_LIK_MVN) {
     if (DMAX <= 16) {
       if (b.gradient_guided || b.gradient_slice)
-        k_slice_shell<DM, GBNS_LIK_MVN, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
-      else k_slice_shell<DM, GBNS_LIK_MVN, false><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+        return launch_slice_kernel(k_slice_shell<DM, GBNS_LIK_MVN, true>, DM, nblk, threads, b, ib, Lstar, keys, stream);
+      return launch_slice_kernel(k_slice_shell<DM, GBNS_LIK_MVN, false>, DM, nblk, threads, b, ib, Lstar, keys, stream);
     }
   } else {
     if (b.gradient_guided || b.gradient_slice)
-      k_slice_shell<DMAX, GBNS_LIK_SHELLS, true><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
-    else k_slice_shell<DMAX, GBNS_LIK_SHELLS, false><<<nblk, threads, 0, stream>>>(b, ib, Lstar, keys);
+      return launch_slice_kernel(k_slice_shell<DMAX, GBNS_LIK_SHELLS, true>, DMAX, nblk, threads, b, ib, Lstar, keys,
+                                 stream);
+    return launch_slice_kernel(k_slice_shell<DMAX, GBNS_LIK_SHELLS, false>, DMAX, nblk, threads, b, ib, Lstar, keys,
+                               stream);
   }
   return cudaGetLastError();
 }
