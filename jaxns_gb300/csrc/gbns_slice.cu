@@ -132,14 +132,15 @@ __device__ __forceinline__ float slice_alpha(int j, int S) {
   return 0.5f * (1.0f - step) + step;
 }
 
-// Minimum resident CTAs per SM (8 caps registers at 64): the sampler is latency-bound, and
-// at DMAX <= 8 the cap costs a few tens of bytes of spills per thread; Gaussian shells at
-// DMAX 16 runs fastest at 6 CTAs (80 registers, 52 B of spills): 2.8 % faster than at 8 CTAs
-// (64 registers, 194 B of spills) and 8 % faster than at its natural 112 registers.  The
-// other instantiations keep the occupancy they reach without a cap (3 or 4 CTAs).
+// Minimum resident 128-thread CTAs per SM (8 caps registers at 64): the sampler is latency-
+// bound, and at DMAX <= 8 the cap costs a few tens of bytes of spills per thread.  Gaussian
+// shells at DMAX 16 run fastest at 7 (72 registers, 32 B of spills): 3.8 % faster than at 6
+// (80 registers) once the direction scratch is sized per warp, so that shared memory no longer
+// limits the resident CTAs.  The other instantiations keep the occupancy they reach without a
+// cap (3 or 4 CTAs).
 template <int DMAX, int FAM>
 constexpr int slice_min_blocks() {
-  return DMAX <= 8 ? 8 : ((DMAX == 16 && FAM == GBNS_LIK_SHELLS) ? 6 : (DMAX >= 64 ? 3 : 4));
+  return DMAX <= 8 ? 8 : ((DMAX == 16 && FAM == GBNS_LIK_SHELLS) ? 7 : (DMAX >= 64 ? 3 : 4));
 }
 
 // GRAD: the gradient instantiation, for UniDimSliceSampler's two gradient options (runtime
