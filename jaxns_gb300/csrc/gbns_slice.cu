@@ -133,14 +133,15 @@ __device__ __forceinline__ float slice_alpha(int j, int S) {
 }
 
 // Minimum resident 128-thread CTAs per SM (8 caps registers at 64): the sampler is latency-
-// bound, and at DMAX <= 8 the cap costs a few tens of bytes of spills per thread.  Gaussian
+// bound, and at DMAX <= 8 the cap costs a few tens of bytes of spills per thread (correlated
+// Gaussians at D <= 8: 7 is 0.8 % faster than 8 and 6 is 18 % slower).  Gaussian
 // shells at DMAX 16 run fastest at 7 (72 registers, 32 B of spills): 3.8 % faster than at 6
 // (80 registers) once the direction scratch is sized per warp, so that shared memory no longer
 // limits the resident CTAs.  The other instantiations keep the occupancy they reach without a
 // cap (3 or 4 CTAs).
 template <int DMAX, int FAM>
 constexpr int slice_min_blocks() {
-  return DMAX <= 8 ? 8 : ((DMAX == 16 && FAM == GBNS_LIK_SHELLS) ? 7 : (DMAX >= 64 ? 3 : 4));
+  return DMAX <= 8 ? (FAM == GBNS_LIK_MVN ? 7 : 8) : ((DMAX == 16 && FAM == GBNS_LIK_SHELLS) ? 7 : (DMAX >= 64 ? 3 : 4));
 }
 
 // GRAD: the gradient instantiation, for UniDimSliceSampler's two gradient options (runtime
