@@ -38,7 +38,8 @@ __device__ float loglik_generic(const gbns_batch &b, const gbns_run_desc &rd, co
       r2 = fmaf(e2, e2, r2);
     }
     const float R = fp[2 * D], w = fp[2 * D + 1];
-    const float z1 = (sqrtf(r1) - R) / w, z2 = (sqrtf(r2) - R) / w;
+    const float iw = 1.0f / w;  // the shell width's reciprocal, as the sampler kernel forms it
+    const float z1 = (sqrtf(r1) - R) * iw, z2 = (sqrtf(r2) - R) * iw;
     const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
     const float m = fmaxf(s1, s2), dd = s1 - s2;
     v = (dd != dd) ? s1 + s2 : m + gbns_fm_log1p(gbns_fm_exp(-fabsf(dd)));

@@ -20,6 +20,7 @@ struct RunSmem {
   float p0[DMAX];                       // MVN: mu      SHELLS: c1
   float p1[FAM == GBNS_LIK_MVN ? DMAX * DMAX : DMAX];  // MVN: Linv   SHELLS: c2
   float c0, R, w, norm;
+  float iw;                             // SHELLS: 1 / w (correctly rounded)
   int m;                                // live points above the contour
 };
 
@@ -116,7 +117,7 @@ __device__ __forceinline__ float loglik(const RunSmem<DMAX, FAM> &P, int D, cons
         r2 = fmaf(e2, e2, r2);
       }
     }
-    const float z1 = (sqrtf(r1) - P.R) / P.w, z2 = (sqrtf(r2) - P.R) / P.w;
+    const float z1 = (sqrtf(r1) - P.R) * P.iw, z2 = (sqrtf(r2) - P.R) * P.iw;
     const float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
     const float m = fmaxf(s1, s2), dd = s1 - s2;
     v = (dd != dd) ? s1 + s2 : m + gbns_fm_log1p(gbns_fm_exp(-fabsf(dd)));
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
     } else {
       P.R = fp[2 * D];
       P.w = fp[2 * D + 1];
+      P.iw = 1.0f / P.w;
       P.norm = fp[2 * D + 2];
     }
     // m = #live points with log L > L* (the live set is sorted ascending)

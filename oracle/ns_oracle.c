@@ -1339,7 +1339,8 @@ static float o32_loglik_line(const orc32_model *m, const float *u0, const float 
             r1 = fmaf(e1, e1, r1);
             r2 = fmaf(e2, e2, r2);
         }
-        float z1 = (sqrtf(r1) - R) / w, z2 = (sqrtf(r2) - R) / w;
+        float iw = 1.0f / w; /* the kernels multiply by the width's reciprocal */
+        float z1 = (sqrtf(r1) - R) * iw, z2 = (sqrtf(r2) - R) * iw;
         float s1 = -0.5f * z1 * z1, s2 = -0.5f * z2 * z2;
         float mx = fmaxf(s1, s2), dd = s1 - s2;
         v = (dd != dd) ? s1 + s2 : mx + gbns_fm_log1p(gbns_fm_exp(-fabsf(dd)));
