@@ -6,6 +6,7 @@ import os
 import subprocess
 import sys
 
+import numpy as np
 import pytest
 
 from tests.conftest import ROOT
@@ -54,3 +55,21 @@ def test_reference_arm_prints_one_line():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["unit"] == "runs/s" and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+
+
+def test_plain_sample_is_stratified_by_dimension():
+    """The plain single-run comparison times one run per equal-width stratum of D, weighted by
+    the stratum's run count (a run's cost grows steeply with D); a single-dimension batch gives
+    evenly spaced runs of equal weight."""
+    import bench
+    wl = bench.workload(4096, 2024, "config3")
+    Ds = np.array([w[0] for w in wl])
+    idx, weight = bench.plain_sample(Ds)
+    assert len(idx) == 8 and sum(weight) == len(wl)
+    edges = np.linspace(Ds.min(), Ds.max() + 1, 9)
+    for k, (r, wt) in enumerate(zip(idx, weight)):
+        assert edges[k] <= Ds[r] < edges[k + 1]
+        assert wt == np.count_nonzero((Ds >= edges[k]) & (Ds < edges[k + 1]))
+    assert min(Ds[idx]) <= 8 and max(Ds[idx]) >= 58  # the sample reaches both ends of D
+    idx, weight = bench.plain_sample(np.full(1024, 10))
+    assert idx == list(range(0, 1024, 128)) and weight == [128.0] * 8

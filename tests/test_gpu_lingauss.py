@@ -391,3 +391,26 @@ def test_lingauss_gradient_guided_evidence(gpu_lib):
     res = ns.to_results(reason, state)
     truth, _ = blr_log_evidence(Phi, y, 0.0, np.log(0.5))
     assert abs(res.log_Z_mean - truth) < 4 * res.log_Z_uncert + 0.05, (res.log_Z_mean, res.log_Z_uncert, truth)
+
+
+def test_lingauss_gradient_options_refuse_fused_shell(gpu_lib):
+    """The fused shell does not take the slice sampler's gradient options: the engine refuses
+    lg_fused=True with them and otherwise picks the lock step, and the fused C entry point
+    refuses a batch that has them set."""
+    import ctypes
+    import jaxns_gb300 as gb
+    from jaxns_gb300 import _ffi
+    from jaxns_gb300.engine import NSBatch
+    Phi, y = blr(500, 6, seed=4)
+    ns = gb.NestedSampler(blr_model(gb, Phi, y), num_live_points=100, num_slices=6)
+    spec = ns.nested_sampler.run_spec(gb.random.PRNGKey(9), ns.normalise_term_cond(None))
+    fused = NSBatch([spec], lg_fused=True)
+    assert fused.lg_fused
+    spec.gradient_guided = True
+    with pytest.raises(ValueError, match="lock step"):
+        NSBatch([spec], lg_fused=True)
+    assert not NSBatch([spec]).lg_fused
+    fused._b.gradient_guided = 1
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    with pytest.raises(_ffi.GBNSError, match="gradient"):
+        _ffi.call("gbns_lg_shell_fused", ctypes.byref(fused._b), ctypes.byref(fused._lgb), stream)
