@@ -150,8 +150,9 @@ __device__ void cta_bitonic(unsigned long long *k, int NP) {
   for (int size = 2; size <= NP; size <<= 1) {
     for (int stride = size >> 1; stride > 0; stride >>= 1) {
       __syncthreads();
+      const int lg = __ffs(stride) - 1;  // stride is a power of two
       for (int t = threadIdx.x; t < NP / 2; t += blockDim.x) {
-        const int lo = 2 * stride * (t / stride) + (t % stride);
+        const int lo = ((t >> lg) << (lg + 1)) + (t & (stride - 1));
         const int hi = lo + stride;
         const bool up = ((lo & size) == 0);
         const unsigned long long a = k[lo], c = k[hi];
@@ -355,8 +356,10 @@ __global__ void __launch_bounds__(128) k_merge(gbns_batch b) {
   for (int i = threadIdx.x; i < NP; i += blockDim.x)
     sk[i] = i < n ? sort_key(i < s ? nL[i] : L[i], i) : ~0ull;
   cta_bitonic(sk, NP);
-  for (long long q = threadIdx.x; q < (long long)n * W; q += blockDim.x) {
-    const int i = (int)(q / W), j = (int)(q % W);
+  // row i = q / W as a multiply-high: exact for q < 2^25 and W <= 128 (n W <= 4096 x 128)
+  const uint32_t wmagic = W > 1 ? (uint32_t)(((1ull << 32) + (uint64_t)W - 1ull) / (uint64_t)W) : 0u;
+  for (int q = threadIdx.x; q < n * W; q += blockDim.x) {
+    const int i = W > 1 ? (int)__umulhi((uint32_t)q, wmagic) : q, j = q - i * W;
     const int src = (int)(sk[i] & 0xffffffffu);
     oU[(long long)i * W + j] = src < s ? nU[(long long)src * W + j] : U[(long long)src * W + j];
   }
