@@ -131,7 +131,7 @@ def make_samplers(wl):
                     x = yield gb.Prior(gb.MultivariateNormalTriL(pm, pL), name="x")
                     return x
                 cache["gh168"] = gb.Model(prior_model, gb.MultivariateNormalLikelihood(dm, dc))
-            samplers.append(gb.NestedSampler(cache["gh168"], max_samples=cap, store_U=False))
+            samplers.append(gb.NestedSampler(cache["gh168"], max_samples=cap))
             continue
         if kind == "shells":
             if "shells" not in cache:
@@ -145,7 +145,7 @@ def make_samplers(wl):
                 x = yield gb.Prior(gb.Uniform(-10.0 * np.ones(D), 10.0 * np.ones(D)), name="x")
                 return x
             model = gb.Model(prior_model, gb.MultivariateNormalLikelihood(*params))
-        samplers.append(gb.NestedSampler(model, num_live_points=n, num_slices=S, max_samples=cap, store_U=False))
+        samplers.append(gb.NestedSampler(model, num_live_points=n, num_slices=S, max_samples=cap))
     return samplers
 
 
@@ -350,13 +350,22 @@ def main():
             if step >= args.warmup:
                 vals.append(v)
         v = float(np.mean(vals))
-        print(json.dumps({"metric": METRIC, "value": v, "unit": "runs/s", "impl": "reference", "n_gpus": args.gpus,
-                          "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                          "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-                          "config": {"workload": wdesc, "runs": args.runs},
-                          "cpu_baseline": {"value": v, "unit": "runs/s", "cores": threads, "kind": "port",
-                                           "sample": info["sample"]},
-                          "e2e": {"value": v, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        ref_line = {"metric": METRIC, "value": v, "unit": "runs/s", "impl": "reference", "n_gpus": args.gpus,
+                    "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+                    "config": {"workload": wdesc, "runs": args.runs},
+                    "cpu_baseline": {"value": v, "unit": "runs/s", "cores": threads, "kind": "port",
+                                     "sample": info["sample"]},
+                    "e2e": {"value": v, "unit": "runs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        if "log_Z" in info:
+            # accuracy of these runs (seeds PRNGKey(0..k-1), the GPU line's reference_accuracy seeds)
+            t = shells_log_Z() if args.workload == "shells" else gh168_log_Z(*wl[0][2])
+            dz = np.asarray(info["log_Z"]) - t
+            ref_line["accuracy"] = {"truth": "FP64 radial quadrature" if args.workload == "shells" else "analytic",
+                                    "runs": len(dz), "seeds": f"PRNGKey(0..{len(dz) - 1})",
+                                    "frac_abs_dlogZ_lt_0.1": float(np.mean(np.abs(dz) < 0.1)),
+                                    "mean_error": float(np.mean(dz)), "mean_abs_dlogZ": float(np.mean(np.abs(dz)))}
+        print(json.dumps(ref_line))
         return
 
     import torch
