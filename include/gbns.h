@@ -375,6 +375,26 @@ int gbns_evidence_adjoint_tc(const double *U_dev, const double *log_w_dev, long 
  * counts and log-likelihoods (FP64), M < 2^32; log_Z_dev: [S]. */
 int gbns_sample_evidence(const uint32_t *key_dev, const int *num_live_dev, const double *log_L_dev, long long M,
                          int S, double *log_Z_dev, void *stream);
+/* The prior of a model, one entry per U dimension (device pointers), for gbns_prior_transform. */
+typedef struct {
+    int D;
+    const int *kind;        /* [D] gbns_prior */
+    const double *a, *b;    /* [D] Uniform: low, high - low; Normal: loc, scale */
+    const double *log_norm; /* [D] the density's constant: -log b (Uniform), -log b - log(2 pi) / 2 (Normal) */
+    const double *A;        /* [D, D] row-major lower-triangular map X = A q + c over the
+                               MultivariateNormalTriL blocks (q their standard normals), or NULL: X = q */
+    const int *row_start;   /* [D] first column of row d's nonzeros in A (with A) */
+    const double *c;        /* [D] (with A) */
+    double log_det;         /* added to every log density: -sum log L_ii over the blocks */
+} gbns_prior_table;
+
+/* Model.transform and Model.log_prob_prior (framework/model.py:155-187) of M sample rows, as
+ * _to_results applies them to the sorted samples (sharded_static.py:744-745): U is fp32
+ * (U32_dev) or FP64 (U64_dev, the linear-Gaussian family), exactly one of them given, [M, D]
+ * row-major; X_dev [M, D] FP64 or NULL; log_density_dev [M] FP64 or NULL receives
+ * log_L_dev[i] + log p(X_i) (log_L_dev NULL: the prior density alone).  D <= 3600 with A. */
+int gbns_prior_transform(const gbns_prior_table *prior, const float *U32_dev, const double *U64_dev, long long M,
+                         const double *log_L_dev, double *X_dev, double *log_density_dev, void *stream);
 /* compute_evidence_stats over one sorted sample set: ncoef_dev is a coefficient table of nmax + 1
  * rows (GBNS_NCOEF_STRIDE) */
 int gbns_evidence_stats(const float *log_L_dev, const int *num_live_dev, long long N, const double *ncoef_dev,

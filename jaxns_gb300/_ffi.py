@@ -85,13 +85,19 @@ class ResultsBufs(ctypes.Structure):
                 ("U_sorted", c_void_p), ("scalars", c_void_p), ("scratch_ll", c_void_p), ("scratch_i", c_void_p)]
 
 
+class PriorTable(ctypes.Structure):
+    _fields_ = [("D", c_int), ("kind", c_void_p), ("a", c_void_p), ("b", c_void_p), ("log_norm", c_void_p),
+                ("A", c_void_p), ("row_start", c_void_p), ("c", c_void_p), ("log_det", ctypes.c_double)]
+
+
 EXPORTED = ("gbns_version", "gbns_last_error", "gbns_abi_sizes", "gbns_threefry2x32", "gbns_threefry_split", "gbns_random_bits64",
             "gbns_uniform", "gbns_normal", "gbns_forward", "gbns_batch_init", "gbns_batch_iterate",
             "gbns_batch_finalize", "gbns_batch_results", "gbns_slice_shell", "gbns_count_crossed_edges",
             "gbns_evidence_stats", "gbns_batch_shell", "gbns_batch_merge", "gbns_record_event",
             "gbns_count_crossed_edges_static", "gbns_lg_shell_begin", "gbns_lg_steps", "gbns_evidence_adjoint",
             "gbns_lg_prepare_tc", "gbns_evidence_adjoint_tc", "gbns_lg_chain_step", "gbns_lg_residual",
-            "gbns_sample_evidence", "gbns_lg_shell_fused", "gbns_lg_iterate", "gbns_lg_fused_max_clusters")
+            "gbns_sample_evidence", "gbns_lg_shell_fused", "gbns_lg_iterate", "gbns_lg_fused_max_clusters",
+            "gbns_prior_transform")
 
 _lib = None
 

@@ -49,6 +49,7 @@ ARGTYPES = {
     "gbns_evidence_adjoint_tc": [P, P, c_longlong, c_int, P, P, c_int, c_double, c_double, P, P, P, P, P, P, P],
     "gbns_sample_evidence": [P, P, P, c_longlong, c_int, P, P],
     "gbns_evidence_stats": [P, P, c_longlong, P, c_int, P, P, P, P, P],
+    "gbns_prior_transform": [P, P, P, c_longlong, P, P, P, P],
 }
 RESTYPES = {"gbns_last_error": c_char_p}
 

@@ -182,4 +182,16 @@ int gbns_sample_evidence(const uint32_t *key_dev, const int *num_live_dev, const
                "gbns_sample_evidence");
 }
 
+int gbns_prior_transform(const gbns_prior_table *prior, const float *U32_dev, const double *U64_dev, long long M,
+                         const double *log_L_dev, double *X_dev, double *log_density_dev, void *stream) {
+  if (!prior || M < 0 || prior->D <= 0 || (M > 0 && ((U32_dev == nullptr) == (U64_dev == nullptr))) ||
+      !prior->kind || !prior->a || !prior->b || !prior->log_norm)
+    return fail(-1, "gbns_prior_transform: bad arguments%s");
+  if (prior->A && (!prior->row_start || !prior->c || prior->D > 3600))
+    return fail(-1, "gbns_prior_transform: an affine map needs row_start and c, and D <= 3600%s");
+  return check(gbns::launch_prior_transform(*prior, U32_dev, U64_dev, M, log_L_dev, X_dev, log_density_dev,
+                                            (cudaStream_t)stream),
+               "gbns_prior_transform");
+}
+
 }  // extern "C"

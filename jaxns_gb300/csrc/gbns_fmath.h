@@ -23,6 +23,9 @@
  *                     sqrt(2) erfinv(u) with u = (4M + 1 - 2^53) 2^-53 = 2p - 1, so the
  *                     quantile of p = (4M + 1) 2^-54, whose offset from 1/2 and whose tail
  *                     mass are formed exactly in integers and rounded once to fp32.
+ *   gbns_fm_log64, gbns_fm_ndtri64  the FP64 log (the reduction of gbns_fm_log with a longer
+ *                     atanh series) and the AS 241 double-precision quantile PPND16, for the
+ *                     results' U -> X transform and prior density.
  */
 #ifndef GBNS_FMATH_H
 #define GBNS_FMATH_H
@@ -185,6 +188,138 @@ GBNS_FM_FN float gbns_fm_ndtri_d(double u) {
     const double q = u - 0.5;
     if (fabs(q) <= 0.425) return gbns_fm_ndtri_center((float)q);
     const float z = gbns_fm_ndtri_upper((float)(q < 0.0 ? u : 1.0 - u));
+    return q < 0.0 ? -z : z;
+}
+
+/* ---- FP64: the results' prior transform (U -> X) ---------------------------------------- */
+
+GBNS_FM_FN uint64_t gbns_fm_bits64(double x) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(x);
+#else
+    uint64_t u;
+    memcpy(&u, &x, sizeof u);
+    return u;
+#endif
+}
+
+GBNS_FM_FN double gbns_fm_from_bits64(uint64_t u) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)u);
+#else
+    double x;
+    memcpy(&x, &u, sizeof x);
+    return x;
+#endif
+}
+
+/* log(x) in FP64: x = 2^e m with m in [sqrt(2)/2, sqrt(2)), s = (m-1)/(m+1),
+ * log m = 2 atanh(s) = 2s + s^3 sum_{k>=1} 2/(2k+1) s^(2k-2) through k = 10 (|s| <= 0.1716, so the
+ * next term is below 2^-60 of the sum), e ln2 with ln2 split into a 32-bit head and a tail. */
+GBNS_FM_FN double gbns_fm_log64(double x) {
+    if (!(x > 0.0)) return x == 0.0 ? -INFINITY : NAN;
+    if (x == INFINITY) return x;
+    int e = 0;
+    uint64_t ix = gbns_fm_bits64(x);
+    if ((ix >> 52) == 0) { /* subnormal */
+        ix = gbns_fm_bits64(x * 0x1p+54);
+        e = -54;
+    }
+    e += (int)(ix >> 52) - 1023;
+    ix = (ix & 0x000FFFFFFFFFFFFFull) | 0x3FF0000000000000ull; /* m in [1, 2) */
+    if (ix > 0x3FF6A09E667F3BCCull) {                           /* m > sqrt(2): use m / 2 */
+        ix -= 0x0010000000000000ull;
+        e += 1;
+    }
+    const double m = gbns_fm_from_bits64(ix);
+    const double f = m - 1.0; /* exact */
+    const double s = f / (2.0 + f);
+    const double z = s * s;
+    double P = 2.0 / 21.0;
+    P = fma(P, z, 2.0 / 19.0);
+    P = fma(P, z, 2.0 / 17.0);
+    P = fma(P, z, 2.0 / 15.0);
+    P = fma(P, z, 2.0 / 13.0);
+    P = fma(P, z, 2.0 / 11.0);
+    P = fma(P, z, 2.0 / 9.0);
+    P = fma(P, z, 2.0 / 7.0);
+    P = fma(P, z, 2.0 / 5.0);
+    P = fma(P, z, 2.0 / 3.0);
+    const double lm = fma(s * z, P, 2.0 * s);
+    const double ef = (double)e;
+    return fma(ef, 0x1.62e42ffp-1, fma(ef, -0x1.718432a1b0e26p-35, lm));
+}
+
+/* Phi^-1(p) in FP64, p in [0, 1]: AS 241 (Wichura 1988), the double-precision rational
+ * approximations PPND16 (about 1e-16 relative): a degree-7 / degree-7 rational in
+ * r = 0.180625 - q^2 for |q| = |p - 1/2| <= 0.425, else two degree-7 / degree-7 rationals in
+ * r = sqrt(-log(min(p, 1 - p))), split at r = 5.  Horner steps are explicit FMAs, so host and
+ * device give the same bits. */
+GBNS_FM_FN double gbns_fm_ndtri64(double p) {
+    if (!(p == p)) return p;
+    const double q = p - 0.5;
+    if (fabs(q) <= 0.425) {
+        const double r = fma(-q, q, 0.180625);
+        double a = 2.5090809287301226727e+3;
+        a = fma(a, r, 3.3430575583588128105e+4);
+        a = fma(a, r, 6.7265770927008700853e+4);
+        a = fma(a, r, 4.5921953931549871457e+4);
+        a = fma(a, r, 1.3731693765509461125e+4);
+        a = fma(a, r, 1.9715909503065514427e+3);
+        a = fma(a, r, 1.3314166789178437745e+2);
+        a = fma(a, r, 3.3871328727963666080e+0);
+        double b = 5.2264952788528545610e+3;
+        b = fma(b, r, 2.8729085735721942674e+4);
+        b = fma(b, r, 3.9307895800092710610e+4);
+        b = fma(b, r, 2.1213794301586595867e+4);
+        b = fma(b, r, 5.3941960214247511077e+3);
+        b = fma(b, r, 6.8718700749205790830e+2);
+        b = fma(b, r, 4.2313330701600911252e+1);
+        b = fma(b, r, 1.0);
+        return (q * a) / b;
+    }
+    const double t = q < 0.0 ? p : 1.0 - p; /* 1 - p is exact for p > 0.925 */
+    if (!(t > 0.0)) return q < 0.0 ? -INFINITY : INFINITY;
+    double r = sqrt(-gbns_fm_log64(t));
+    double a, b;
+    if (r <= 5.0) {
+        r = r - 1.6;
+        a = 7.74545014278341407640e-4;
+        a = fma(a, r, 2.27238449892691845833e-2);
+        a = fma(a, r, 2.41780725177450611770e-1);
+        a = fma(a, r, 1.27045825245236838258e+0);
+        a = fma(a, r, 3.64784832476320460504e+0);
+        a = fma(a, r, 5.76949722146069140550e+0);
+        a = fma(a, r, 4.63033784615654529590e+0);
+        a = fma(a, r, 1.42343711074968357734e+0);
+        b = 1.05075007164441684324e-9;
+        b = fma(b, r, 5.47593808499534494600e-4);
+        b = fma(b, r, 1.51986665636164571966e-2);
+        b = fma(b, r, 1.48103976427480074590e-1);
+        b = fma(b, r, 6.89767334985100004550e-1);
+        b = fma(b, r, 1.67638483018380384940e+0);
+        b = fma(b, r, 2.05319162663775882187e+0);
+        b = fma(b, r, 1.0);
+    } else {
+        r = r - 5.0;
+        a = 2.01033439929228813265e-7;
+        a = fma(a, r, 2.71155556874348757815e-5);
+        a = fma(a, r, 1.24266094738807843860e-3);
+        a = fma(a, r, 2.65321895265761230930e-2);
+        a = fma(a, r, 2.96560571828504891230e-1);
+        a = fma(a, r, 1.78482653991729133580e+0);
+        a = fma(a, r, 5.46378491116411436990e+0);
+        a = fma(a, r, 6.65790464350110377720e+0);
+        b = 2.04426310338993978564e-15;
+        b = fma(b, r, 1.42151175831644588870e-7);
+        b = fma(b, r, 1.84631831751005468180e-5);
+        b = fma(b, r, 7.86869131145613259100e-4);
+        b = fma(b, r, 1.48753612908506148525e-2);
+        b = fma(b, r, 1.36929880922735805310e-1);
+        b = fma(b, r, 5.99832206555887937690e-1);
+        b = fma(b, r, 1.0);
+    }
+    const double z = a / b;
     return q < 0.0 ? -z : z;
 }
 

@@ -41,6 +41,8 @@ cudaError_t launch_adjoint_tc(const double *U, const double *log_w, long long M,
                               double *ry, float *w_scratch, float *phi_scratch, int *status, cudaStream_t stream);
 cudaError_t launch_sample_evidence(const uint32_t *key, const int *num_live, const double *log_L, long long M, int S,
                                    double *out, cudaStream_t stream);
+cudaError_t launch_prior_transform(const gbns_prior_table &t, const float *U32, const double *U64, long long M,
+                                   const double *log_L, double *X, double *out, cudaStream_t stream);
 // Sets the thread-local message returned by gbns_last_error().
 void record_error(const char *msg);
 cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, void *out, long long n,

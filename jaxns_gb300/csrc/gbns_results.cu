@@ -476,6 +476,89 @@ __global__ void __launch_bounds__(1024) k_sample_evidence(const uint32_t *key, c
   }
 }
 
+// ------------------------------------------------------- prior transform ----
+
+// Model.transform and Model.log_prob_prior (framework/model.py:155-187) over the sorted samples
+// of _to_results (sharded_static.py:744-745), FP64: one warp per sample row, dimensions strided
+// over the lanes (coalesced row reads).  Uniform q = a + b u, Normal q = a + b Phi^-1(u) (AS 241
+// PPND16); with an affine map, X_d = c_d + sum_{k = row_start_d}^{d} A_dk q_k over q staged in
+// shared memory (the MultivariateNormalTriL blocks), else X = q.  The density is each
+// dimension's constant plus -z^2 / 2 (Normal) or 0 / -inf (Uniform, inside / outside), summed
+// per lane in dimension order and then over the warp by the xor butterfly, plus log_det and,
+// when given, log L (the log posterior density).
+template <typename UT>
+__global__ void __launch_bounds__(256) k_prior_transform(gbns_prior_table t, const UT *U, long long M,
+                                                         const double *log_L, double *X, double *out) {
+  extern __shared__ double qs_all[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int D = t.D;
+  double *qs = qs_all + (size_t)warp * D;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long row = (long long)blockIdx.x * (blockDim.x >> 5) + warp; row < M; row += nwarps) {
+    const UT *u_row = U + row * D;
+    double *x_row = X ? X + row * D : nullptr;
+    double lp = 0.0;
+    for (int d = lane; d < D; d += 32) {
+      const double u = (double)u_row[d];
+      const double a = t.a[d], b = t.b[d];
+      double q, ld;
+      if (t.kind[d] == GBNS_PRIOR_NORMAL) {
+        const double z = gbns_fm_ndtri64(u);
+        q = fma(b, z, a);
+        ld = fma(-0.5 * z, z, t.log_norm[d]);
+      } else {
+        q = fma(b, u, a);
+        ld = (q >= a && q <= a + b) ? t.log_norm[d] : -INFINITY;
+      }
+      lp += ld;
+      if (t.A) qs[d] = q;
+      else if (x_row) x_row[d] = q;
+    }
+    if (t.A) {
+      __syncwarp();
+      if (x_row) {
+        for (int d = lane; d < D; d += 32) {
+          const double *a_row = t.A + (size_t)d * D;
+          double acc = t.c[d];
+          const int k0 = t.row_start[d] > 0 ? t.row_start[d] : 0;  // k stays in [0, d]
+          for (int k = k0; k <= d; ++k) acc = fma(a_row[k], qs[k], acc);
+          x_row[d] = acc;
+        }
+      }
+      __syncwarp();
+    }
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) lp += __shfl_xor_sync(0xffffffffu, lp, m);
+    if (lane == 0 && out) out[row] = (log_L ? log_L[row] : 0.0) + (lp + t.log_det);
+  }
+}
+
+cudaError_t launch_prior_transform(const gbns_prior_table &t, const float *U32, const double *U64, long long M,
+                                   const double *log_L, double *X, double *out, cudaStream_t stream) {
+  if (M <= 0) return cudaSuccess;
+  const size_t smem = t.A ? (size_t)8 * t.D * sizeof(double) : 0;
+  int dev = 0, sms = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  const long long want = (M + 7) / 8;
+  const unsigned grid = (unsigned)(want < (long long)sms * 8 ? want : (long long)sms * 8);
+  if (U32) {
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_prior_transform<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem)) != cudaSuccess)
+      return e;
+    k_prior_transform<float><<<grid, 256, smem, stream>>>(t, U32, M, log_L, X, out);
+  } else {
+    if (smem > 48 * 1024 &&
+        (e = cudaFuncSetAttribute(k_prior_transform<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem)) != cudaSuccess)
+      return e;
+    k_prior_transform<double><<<grid, 256, smem, stream>>>(t, U64, M, log_L, X, out);
+  }
+  return cudaGetLastError();
+}
+
 cudaError_t launch_sample_evidence(const uint32_t *key, const int *num_live, const double *log_L, long long M, int S,
                                    double *out, cudaStream_t stream) {
   if (S > 0) k_sample_evidence<<<S, 1024, 0, stream>>>(key, num_live, log_L, M, out);

@@ -150,7 +150,10 @@ class Model:
 
     def transform(self, U):
         """U -> X (dict of prior name -> value), vectorised over leading axes."""
-        X = self.transform_flat(U)
+        return self.unflatten(self.transform_flat(U))
+
+    def unflatten(self, X):
+        """The named priors' views of a flat X [..., D]."""
         return {p.name: X[..., p.start:p.start + p.size].reshape(X.shape[:-1] + tuple(p.shape))
                 for p in self.priors if not p.name.startswith("__prior_")}
 
@@ -173,15 +176,82 @@ class Model:
 
     def transform_flat(self, U):
         import torch
+        if isinstance(U, torch.Tensor) and U.is_cuda:
+            return self.transform_device(U)[0]
         is_t = isinstance(U, torch.Tensor)
         Ut = U if is_t else torch.as_tensor(np.asarray(U, np.float64))
         X = self._quantiles(Ut)[1]
         return X if is_t else X.numpy()
 
+    def _prior_table(self, device):
+        """The per-dimension prior table of gbns_prior_transform, as device tensors (cached)."""
+        import torch
+        cache = getattr(self, "_table_cache", None)
+        if cache is not None and cache[0] == device:
+            return cache[1]
+        D = self.U_ndims
+        normal = self.prior_kind == PRIOR_NORMAL
+        log_norm = -np.log(self.prior_b) - np.where(normal, 0.5 * np.log(2.0 * np.pi), 0.0)
+        t = {"kind": torch.as_tensor(self.prior_kind.astype(np.int32), device=device),
+             "a": torch.as_tensor(self.prior_a, dtype=torch.float64, device=device),
+             "b": torch.as_tensor(self.prior_b, dtype=torch.float64, device=device),
+             "log_norm": torch.as_tensor(log_norm, dtype=torch.float64, device=device),
+             "log_det": 0.0}
+        aff = self.affine()
+        if aff is not None:
+            A, c = aff
+            row_start = np.arange(D, dtype=np.int32)
+            for s0, loc, L in self.tril_blocks:
+                row_start[s0:s0 + len(loc)] = s0
+            t.update(A=torch.as_tensor(A, dtype=torch.float64, device=device),
+                     c=torch.as_tensor(c, dtype=torch.float64, device=device),
+                     row_start=torch.as_tensor(row_start, device=device),
+                     log_det=-float(sum(np.sum(np.log(np.diag(L))) for _, _, L in self.tril_blocks)))
+        self._table_cache = (device, t)
+        return t
+
+    def transform_device(self, U, log_L=None, with_X: bool = True):
+        """(X, log density) of the rows of a CUDA tensor U [..., D] (fp32, or FP64 for the
+        linear-Gaussian family) by the prior-transform kernel: X FP64 [..., D] (None unless
+        with_X) and log L + log p(X) (log_L given) or log p(X), FP64 [...]."""
+        import ctypes
+        import torch
+        from . import _ffi
+        _ffi.require_cuda("Model.transform_device", U=U)
+        D = self.U_ndims
+        if U.shape[-1] != D:
+            raise ValueError(f"U has {U.shape[-1]} columns, the model {D} dimensions")
+        if U.dtype not in (torch.float32, torch.float64):
+            raise ValueError(f"U must be float32 or float64, not {U.dtype}")
+        lead = tuple(U.shape[:-1])
+        Uc = U.reshape(-1, D).contiguous()
+        M = Uc.shape[0]
+        t = self._prior_table(U.device)
+        X = torch.empty((M, D), dtype=torch.float64, device=U.device) if with_X else None
+        out = torch.empty(M, dtype=torch.float64, device=U.device)
+        lL = None
+        if log_L is not None:
+            _ffi.require_cuda("Model.transform_device", log_L=log_L)
+            lL = log_L.reshape(-1).to(torch.float64).contiguous()
+            if lL.numel() != M:
+                raise ValueError(f"log_L has {lL.numel()} entries for {M} rows")
+        p = lambda x: ctypes.c_void_p(x.data_ptr() if x is not None else 0)
+        tab = _ffi.PriorTable(D=D, kind=t["kind"].data_ptr(), a=t["a"].data_ptr(), b=t["b"].data_ptr(),
+                              log_norm=t["log_norm"].data_ptr(), A=t["A"].data_ptr() if "A" in t else None,
+                              row_start=t["row_start"].data_ptr() if "A" in t else None,
+                              c=t["c"].data_ptr() if "A" in t else None, log_det=t["log_det"])
+        f32 = Uc.dtype == torch.float32
+        stream = ctypes.c_void_p(torch.cuda.current_stream(U.device).cuda_stream)
+        _ffi.call("gbns_prior_transform", ctypes.byref(tab), p(Uc if f32 else None), p(None if f32 else Uc),
+                  ctypes.c_longlong(M), p(lL), p(X), p(out), stream)
+        return (X.view(lead + (D,)) if X is not None else None), out.view(lead)
+
     def log_prob_prior(self, U):
         """log prior density of the X that U maps to (per sample); a tensor for a tensor U, a
         numpy array otherwise."""
         import torch
+        if isinstance(U, torch.Tensor) and U.is_cuda:
+            return self.transform_device(U, with_X=False)[1]
         is_t = isinstance(U, torch.Tensor)
         Ut = U if is_t else torch.as_tensor(np.asarray(U, np.float64))
         q, X = self._quantiles(Ut)

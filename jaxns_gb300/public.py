@@ -220,9 +220,8 @@ def results_from_batch(model: Model, batch: NSBatch, r: int, termination_reason:
     sc = v["scalars"].cpu().numpy()
     U = v.get("U_sorted")
     if U is not None:
-        Ud = U.double()
-        samples = model.transform(Ud)
-        lpd = v["log_L_samples"] + model.log_prob_prior(Ud)
+        X, lpd = model.transform_device(U, log_L=v["log_L_samples"])
+        samples = model.unflatten(X)
     else:
         samples, lpd = {}, None
     return NestedSamplerResults(

@@ -1580,3 +1580,52 @@ float orc32_fm_log1p(float x) { return gbns_fm_log1p(x); }
 float orc32_fm_ndtri(float u) { return gbns_fm_ndtri(u); }
 float orc32_fm_ndtri_d(double u) { return gbns_fm_ndtri_d(u); }
 float orc32_fm_normal_from_bits(uint64_t b) { return gbns_fm_normal_from_mantissa(b >> 12); }
+double orc_fm_log64(double x) { return gbns_fm_log64(x); }
+double orc_fm_ndtri64(double p) { return gbns_fm_ndtri64(p); }
+
+/* Model.transform and Model.log_prob_prior (framework/model.py:155-187) of M sample rows, as
+ * _to_results applies them to the sorted samples (sharded_static.py:744-745), in the
+ * arithmetic of the device's prior transform: Uniform q = fma(b, u, a), Normal
+ * q = fma(b, Phi^-1(u), a) with the AS 241 PPND16 quantile, X = c + A q row by row over
+ * [row_start, d] when A is given (the MultivariateNormalTriL blocks), and the density summed
+ * per lane (dimension d on lane d mod 32, in dimension order), then over the 32 lanes by the
+ * xor butterfly, plus log_det and log L when given.  U is fp32 (U32) or FP64 (U64). */
+void orc_prior_transform(int D, const int *kind, const double *a, const double *b, const double *log_norm,
+                         const double *A, const int *row_start, const double *c, double log_det, const float *U32,
+                         const double *U64, long M, const double *log_L, double *X, double *out) {
+    double *q = (double *)malloc(sizeof(double) * (size_t)(D > 0 ? D : 1));
+    for (long row = 0; row < M; ++row) {
+        double part[32], tmp[32];
+        for (int l = 0; l < 32; ++l) part[l] = 0.0;
+        for (int d = 0; d < D; ++d) {
+            const double u = U32 ? (double)U32[row * D + d] : U64[row * D + d];
+            double ld;
+            if (kind[d] == ORC_PRIOR_NORMAL) {
+                const double z = gbns_fm_ndtri64(u);
+                q[d] = fma(b[d], z, a[d]);
+                ld = fma(-0.5 * z, z, log_norm[d]);
+            } else {
+                q[d] = fma(b[d], u, a[d]);
+                ld = (q[d] >= a[d] && q[d] <= a[d] + b[d]) ? log_norm[d] : -INFINITY;
+            }
+            part[d & 31] += ld;
+        }
+        if (X) {
+            for (int d = 0; d < D; ++d) {
+                if (!A) {
+                    X[row * D + d] = q[d];
+                    continue;
+                }
+                double acc = c[d];
+                for (int k = row_start[d] > 0 ? row_start[d] : 0; k <= d; ++k) acc = fma(A[(size_t)d * D + k], q[k], acc);
+                X[row * D + d] = acc;
+            }
+        }
+        for (int m = 16; m >= 1; m >>= 1) {
+            for (int l = 0; l < 32; ++l) tmp[l] = part[l] + part[l ^ m];
+            memcpy(part, tmp, sizeof part);
+        }
+        if (out) out[row] = (log_L ? log_L[row] : 0.0) + (part[0] + log_det);
+    }
+    free(q);
+}

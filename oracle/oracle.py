@@ -129,6 +129,9 @@ def lib():
         _lib.orc32_fm_normal_from_bits.restype = ctypes.c_float
         _lib.orc32_fm_normal_from_bits.argtypes = [ctypes.c_uint64]
         _lib.orc32_forward.restype = ctypes.c_float
+        for nm in ("orc_fm_log64", "orc_fm_ndtri64"):
+            getattr(_lib, nm).restype = ctypes.c_double
+            getattr(_lib, nm).argtypes = [ctypes.c_double]
     return _lib
 
 
@@ -685,3 +688,38 @@ def fm(name, x):
     else:
         vals = [f(float(np.float32(v))) for v in flat]
     return np.array(vals, np.float32).reshape(np.shape(x))
+
+
+# ----------------------------------------------------------------------------- prior transform
+
+def fm_log64(x: float) -> float:
+    return lib().orc_fm_log64(float(x))
+
+
+def fm_ndtri64(p: float) -> float:
+    return lib().orc_fm_ndtri64(float(p))
+
+
+def prior_transform(kind, a, b, log_norm, U, A=None, row_start=None, c=None, log_det=0.0, log_L=None):
+    """Model.transform / Model.log_prob_prior of the rows of U (framework/model.py:155-187) in
+    the device transform's arithmetic: returns (X [M, D] float64, log density [M] float64)."""
+    U = np.ascontiguousarray(U)
+    M, D = U.shape
+    kind = np.ascontiguousarray(kind, np.int32)
+    a, b, log_norm = (np.ascontiguousarray(v, np.float64) for v in (a, b, log_norm))
+    X = np.zeros((M, D), np.float64)
+    out = np.zeros(M, np.float64)
+    U32 = U if U.dtype == np.float32 else None
+    U64 = np.ascontiguousarray(U, np.float64) if U32 is None else None
+    fp = ctypes.POINTER(ctypes.c_float)
+    Ak = np.ascontiguousarray(A, np.float64) if A is not None else None
+    rs = np.ascontiguousarray(row_start, np.int32) if A is not None else None
+    ck = np.ascontiguousarray(c, np.float64) if A is not None else None
+    lL = np.ascontiguousarray(log_L, np.float64) if log_L is not None else None
+    lib().orc_prior_transform(
+        ctypes.c_int(D), _ip(kind), _dp(a), _dp(b), _dp(log_norm),
+        _dp(Ak) if Ak is not None else None, _ip(rs) if rs is not None else None,
+        _dp(ck) if ck is not None else None, ctypes.c_double(log_det),
+        U32.ctypes.data_as(fp) if U32 is not None else None, _dp(U64) if U64 is not None else None,
+        ctypes.c_long(M), _dp(lL) if lL is not None else None, _dp(X), _dp(out))
+    return X, out
