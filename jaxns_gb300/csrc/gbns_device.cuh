@@ -239,7 +239,7 @@ __device__ __forceinline__ ScaledSum ss_sum(ScaledSum a, ScaledSum b) {
 }
 
 struct EvScanSmem {
-  double carry_lX, fin_lX, fin_lX2;
+  double carry_lX, carry_lX2, fin_lX, fin_lX2;
   ScaledSum fin[4];  // A, Z, Z2, dZ2 after the scan
   double last_ldZ;
   float last_L;
@@ -331,6 +331,39 @@ __device__ __forceinline__ void pair_of(double x, float &h, float &l) {
   l = (isinf(h) || isnan(h)) ? 0.0f : __double2float_rn(x - (double)h);
 }
 
+// h + l (an fp32 pair with |l| <= ulp(h) / 2, as pair_sum2 leaves it) as an FP64 value,
+// built with integer operations only (GB300 issues FP64 at about 1/64 of the FP32 rate): h's
+// significand widened to 53 bits plus l's significand aligned to it (bits below 2^-52 of h
+// truncated), renormalised by at most one bit.  Zero, infinities and NaN pass through exactly;
+// a subnormal h (not met by log-space values) takes the FP64 conversion.
+__device__ __forceinline__ double pair_to_double(float h, float l) {
+  const uint32_t hb = __float_as_uint(h);
+  const uint32_t eh = (hb >> 23) & 0xffu;
+  const unsigned long long sign = (unsigned long long)(hb >> 31) << 63;
+  if (eh == 0xffu)
+    return __longlong_as_double((long long)(sign | 0x7ff0000000000000ull |
+                                            ((unsigned long long)(hb & 0x7fffffu) << 29)));
+  if (eh == 0u) return (hb & 0x7fffffffu) == 0u ? __longlong_as_double((long long)sign) : (double)h + (double)l;
+  unsigned long long sig = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;  // units of 2^(e - 52)
+  int e = (int)eh - 127;
+  const uint32_t lb = __float_as_uint(l);
+  const uint32_t el = (lb >> 23) & 0xffu;
+  if (el != 0u && el != 0xffu) {
+    const unsigned long long ml = (lb & 0x7fffffu) | 0x800000u;
+    const int sh = (int)el - 127 - e + 29;  // l = ml 2^(el - 150) in units of 2^(e - 52)
+    const unsigned long long add = sh >= 0 ? (ml << (sh < 40 ? sh : 40)) : (sh > -40 ? (ml >> -sh) : 0ull);
+    sig = ((lb ^ hb) >> 31) ? sig - add : sig + add;
+    if (sig >= (1ull << 53)) {
+      sig >>= 1;
+      e += 1;
+    } else if (sig < (1ull << 52)) {
+      sig <<= 1;
+      e -= 1;
+    }
+  }
+  return __longlong_as_double((long long)(sign | ((unsigned long long)(e + 1023) << 52) | (sig & 0xfffffffffffffull)));
+}
+
 // exp(vh + vl): an exact power of two times exp2f of the fraction (vh + vl) / ln 2 - e
 __device__ __forceinline__ FS fs_term(float vh, float vl) {
   if (!(vh > -INFINITY) || !(vh < INFINITY)) return fs_zero();  // -inf, +inf or NaN: no term
@@ -360,6 +393,31 @@ __device__ __forceinline__ FS fs_sum(FS a, FS b) {
   FS r;
   pair_sum2(a.h, a.l, b.h * sc, b.l * sc, r.h, r.l);
   r.e = a.e;
+  return r;
+}
+
+// a * f for a finite f >= 0: f's exponent moves into e, its significand m in [1, 2) multiplies
+// the pair (TwoProd by FMA); a subnormal or zero f gives zero
+__device__ __forceinline__ FS fs_scale(FS a, float f) {
+  const uint32_t fb = __float_as_uint(f);
+  if (!(a.h > 0.0f) || !(f < INFINITY) || (fb >> 23) == 0u || (fb >> 31)) return fs_zero();
+  const float m = __uint_as_float((fb & 0x7fffffu) | 0x3f800000u);
+  FS r;
+  r.h = a.h * m;
+  r.l = fmaf(a.l, m, fmaf(a.h, m, -r.h));
+  r.e = a.e + (int)(fb >> 23) - 127;
+  return r;
+}
+
+// a * b (TwoProd of the heads by FMA, the cross terms added to the error, renormalised)
+__device__ __forceinline__ FS fs_mul(FS a, FS b) {
+  if (!(a.h > 0.0f) || !(b.h > 0.0f)) return fs_zero();
+  const float p = a.h * b.h;
+  const float lo = fmaf(a.h, b.h, -p) + fmaf(a.h, b.l, a.l * b.h);
+  FS r;
+  r.h = p + lo;
+  r.l = lo - (r.h - p);
+  r.e = a.e + b.e;
   return r;
 }
 
@@ -417,7 +475,7 @@ __device__ __forceinline__ double fs_log_d(FS a) {
 
 struct EvScanFsSmem {
   FS ws[32];
-  FS red[3][32];
+  FS red[5][32];
 };
 
 // CTA scan of pair-scaled values: inclusive and exclusive prefix of each thread's value, and
@@ -492,23 +550,49 @@ __device__ __forceinline__ void cta_scan_p2(float &ah, float &al, float &bh, flo
   __syncthreads();
 }
 
+// The coefficient pairs of one live-point count n: (T, t, T2, t2, tT) as fp32 pairs, bytes
+// 64-103 of the table row (computed in FP64 beyond the table)
+__device__ __forceinline__ void ncoef_pairs(const double *__restrict__ ncoef, int nmax, int nk, float cp[10]) {
+  if (nk <= nmax) {
+    const float4 *c = (const float4 *)(ncoef + (size_t)nk * GBNS_NCOEF_STRIDE + 8);
+    const float4 c0 = c[0], c1 = c[1];
+    const float2 c2 = *(const float2 *)(c + 2);
+    cp[0] = c0.x; cp[1] = c0.y; cp[2] = c0.z; cp[3] = c0.w;
+    cp[4] = c1.x; cp[5] = c1.y; cp[6] = c1.z; cp[7] = c1.w;
+    cp[8] = c2.x; cp[9] = c2.y;
+  } else {
+    double cf[5];
+    ncoef_compute((double)nk, cf);
+#pragma unroll
+    for (int q = 0; q < 5; ++q) pair_of(cf[q], cp[2 * q], cp[2 * q + 1]);
+  }
+}
+
 // Process elements [0, M) of log-likelihoods L (fp32) with live-point counts given by
 // nmode: nconst > 0 -> n_k = nconst; ndesc > 0 -> n_k = ndesc - k; else n_k = narr[k].
 // Called by every thread of the CTA (blockDim a multiple of 32), each holding the same acc.
 // Optional per-element outputs (FP64 logs): log X, log dZ and, with OUT_LZ, the running log Z.
 // L values are relative to Loff (added back in FP64); Lidx, when given, gathers L[Lidx[k]].
-// Inside the loop every thread carries pair copies of log X, log X2, A and Z; thread 0 alone
-// keeps the FP64 carries (in shared memory), which every thread reads back at the end.
-template <bool OUT_LZ>
+// A chunk is K consecutive elements per thread: each thread runs its elements' prefixes
+// sequentially and the CTA scans only the threads' totals (log T and log T2 as fp32 pairs,
+// the affine term c and, with OUT_LZ, dZ as pair-scaled sums).  Every thread carries pair
+// copies of log X and log X2; thread 0 alone keeps the FP64 carries (in shared memory), which
+// every thread reads back after each chunk and at the end.
+// h_out (shared memory, OUT_LZ false only), when given, receives the dZ-weighted means of this
+// scan's samples sum dZ max(L, 0) / sum dZ and sum dZ max(-L, 0) / sum dZ (L relative to
+// Loff), for H.
+template <bool OUT_LZ, int K = 1>
 __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long long M, int nconst, int ndesc,
                                   const int *__restrict__ narr, const double *__restrict__ ncoef, int nmax,
                                   double *__restrict__ out_lX, double *__restrict__ out_ldZ,
                                   double *__restrict__ out_lZ, double Loff, const int *__restrict__ Lidx,
-                                  EvScanSmem &sm) {
+                                  EvScanSmem &sm, double *h_out = nullptr) {
   __shared__ EvScanFsSmem fsm;
   __shared__ EvScanPairSmem psm;
   const int tid = threadIdx.x, T = blockDim.x;
+  const long long CH = (long long)T * K;
   FS pZ = fs_zero(), pZ2 = fs_zero(), pdZ2 = fs_zero();  // this thread's partial sums
+  FS pHP = fs_zero(), pHQ = fs_zero();  // sum dZ L+, dZ L- (h_out)
   float off_h, off_l;
   pair_of(Loff, off_h, off_l);
   const float ln2_h = 0.693147182464599609375f, ln2_l = -1.904654323148236017e-9f;
@@ -516,106 +600,178 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
   pair_of(acc.lX, lxh, lxl);
   pair_of(acc.lX2, lx2h, lx2l);
   FS A0 = fs_from_ss(acc.A), Z0 = fs_from_ss(acc.Z);
-  if (tid == 0) sm.carry_lX = acc.lX;
+  if (tid == 0) {
+    sm.carry_lX = acc.lX;
+    sm.carry_lX2 = acc.lX2;
+  }
   __syncthreads();
-  for (long long base = 0; base < M; base += T) {
-    const long long k = base + tid;
-    const bool valid = k < M;
-    const float Lk = valid ? L[Lidx ? Lidx[k] : k] : 0.0f;
-    const float Lm1 = !valid ? 0.0f : (k == 0 ? acc.Lprev : L[Lidx ? Lidx[k - 1] : k - 1]);
-    int nk = 1;
-    if (valid) nk = nconst > 0 ? nconst : (ndesc > 0 ? (int)(ndesc - k) : narr[k]);
-    nk = nk < 0 ? 0 : nk;
-    // the n-only coefficients (T, t, T2, t2, tT) as fp32 pairs: bytes 64-103 of the table row
-    float cp[10];
-    if (nk <= nmax) {
-      const float4 *c = (const float4 *)(ncoef + (size_t)nk * GBNS_NCOEF_STRIDE + 8);
-      const float4 c0 = c[0], c1 = c[1];
-      const float2 c2 = *(const float2 *)(c + 2);
-      cp[0] = c0.x; cp[1] = c0.y; cp[2] = c0.z; cp[3] = c0.w;
-      cp[4] = c1.x; cp[5] = c1.y; cp[6] = c1.z; cp[7] = c1.w;
-      cp[8] = c2.x; cp[9] = c2.y;
-    } else {
-      double cf[5];
-      ncoef_compute((double)nk, cf);
+  for (long long base = 0; base < M; base += CH) {
+    const long long k0 = base + (long long)tid * K;
+    // (A) inputs, and this thread's running sums of log T and log T2 (pT[j]: through element j)
+    float Lk[K];
+    int nk[K];
+    float pTh[K], pTl[K], pT2h[K], pT2l[K];
+    float Lfirst_m1 = 0.0f;
 #pragma unroll
-      for (int q = 0; q < 5; ++q) pair_of(cf[q], cp[2 * q], cp[2 * q + 1]);
+    for (int j = 0; j < K; ++j) {
+      const long long k = k0 + j;
+      const bool valid = k < M;
+      Lk[j] = valid ? L[Lidx ? Lidx[k] : k] : 0.0f;
+      if (j == 0) Lfirst_m1 = !valid ? 0.0f : (k == 0 ? acc.Lprev : L[Lidx ? Lidx[k - 1] : k - 1]);
+      int n = 1;
+      if (valid) n = nconst > 0 ? nconst : (ndesc > 0 ? (int)(ndesc - k) : narr[k]);
+      nk[j] = n < 0 ? 0 : n;
     }
-    // log X and log X2 of this element: the carried values plus the CTA's pair prefix of
-    // log T and log T2
-    float sTh = valid ? cp[0] : 0.0f, sTl = valid ? cp[1] : 0.0f;
-    float sT2h = valid ? cp[4] : 0.0f, sT2l = valid ? cp[5] : 0.0f;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      float cp[10];
+      ncoef_pairs(ncoef, nmax, nk[j], cp);
+      const bool valid = k0 + j < M;
+      const float th = j == 0 ? 0.0f : pTh[j > 0 ? j - 1 : 0], tl = j == 0 ? 0.0f : pTl[j > 0 ? j - 1 : 0];
+      const float t2h_ = j == 0 ? 0.0f : pT2h[j > 0 ? j - 1 : 0], t2l_ = j == 0 ? 0.0f : pT2l[j > 0 ? j - 1 : 0];
+      pair_sum2(th, tl, valid ? cp[0] : 0.0f, valid ? cp[1] : 0.0f, pTh[j], pTl[j]);
+      pair_sum2(t2h_, t2l_, valid ? cp[4] : 0.0f, valid ? cp[5] : 0.0f, pT2h[j], pT2l[j]);
+    }
+    // CTA prefix of the thread sums; base = the carried log X (log X2) plus the sums of the
+    // elements before this thread's
+    float ah = pTh[K - 1], al = pTl[K - 1], bh = pT2h[K - 1], bl = pT2l[K - 1];
     float4 tot;
-    cta_scan_p2(sTh, sTl, sT2h, sT2l, tot, psm);
-    float xch, xcl, xph, xpl, x2ph, x2pl, eh, el;
-    pair_sum2(lxh, lxl, sTh, sTl, xch, xcl);                          // log X_k
-    pair_sum2(sTh, sTl, valid ? -cp[0] : 0.0f, valid ? -cp[1] : 0.0f, eh, el);
-    pair_sum2(lxh, lxl, eh, el, xph, xpl);                            // log X_{k-1}
-    pair_sum2(sT2h, sT2l, valid ? -cp[4] : 0.0f, valid ? -cp[5] : 0.0f, eh, el);
-    pair_sum2(lx2h, lx2l, eh, el, x2ph, x2pl);                        // log X2_{k-1}
-    // log((L_k + L_{k-1}) / 2) + Loff as a pair: max + log1p(exp(-|d|)) - ln 2 + Loff; -inf
-    // outside the chunk
-    float mh = -INFINITY, ml = 0.0f;
-    if (valid) {
-      const float m = fmaxf(Lk, Lm1), d = Lk - Lm1;
-      if (isnan(d)) {
-        mh = Lk + Lm1;  // both -inf (or +inf)
-      } else {
-        float th, tl;
-        pair_sum2(m, 0.0f, log1pf(__expf(-fabsf(d))), 0.0f, th, tl);
-        pair_sum2(th, tl, -ln2_h, -ln2_l, th, tl);
-        pair_sum2(th, tl, off_h, off_l, mh, ml);
+    cta_scan_p2(ah, al, bh, bl, tot, psm);
+    float bxh, bxl, bx2h, bx2l;
+    pair_sum2(ah, al, -pTh[K - 1], -pTl[K - 1], bxh, bxl);
+    pair_sum2(bh, bl, -pT2h[K - 1], -pT2l[K - 1], bx2h, bx2l);
+    pair_sum2(lxh, lxl, bxh, bxl, bxh, bxl);
+    pair_sum2(lx2h, lx2l, bx2h, bx2l, bx2h, bx2l);
+    // (B) per element, independently: log X, the midpoint, dZ, the affine term c and t2
+    float dzh[K], dzl[K], t2h[K], t2l[K], xch[K], xcl[K];
+    FS cj[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const long long k = k0 + j;
+      const bool valid = k < M;
+      float cp[10];
+      ncoef_pairs(ncoef, nmax, nk[j], cp);
+      float xph = bxh, xpl = bxl, x2ph = bx2h, x2pl = bx2l;  // log X_{k-1}, log X2_{k-1}
+      if (j > 0) {
+        pair_sum2(bxh, bxl, pTh[j > 0 ? j - 1 : 0], pTl[j > 0 ? j - 1 : 0], xph, xpl);
+        pair_sum2(bx2h, bx2l, pT2h[j > 0 ? j - 1 : 0], pT2l[j > 0 ? j - 1 : 0], x2ph, x2pl);
+      }
+      pair_sum2(bxh, bxl, pTh[j], pTl[j], xch[j], xcl[j]);  // log X_k
+      // log((L_k + L_{k-1}) / 2) + Loff as a pair: max + log1p(exp(-|d|)) - ln 2 + Loff; -inf
+      // outside the chunk
+      const float Lcur = Lk[j], Lprev = j == 0 ? Lfirst_m1 : Lk[j > 0 ? j - 1 : 0];
+      float mh = -INFINITY, ml = 0.0f;
+      if (valid) {
+        const float m = fmaxf(Lcur, Lprev), d = Lcur - Lprev;
+        if (isnan(d)) {
+          mh = Lcur + Lprev;  // both -inf (or +inf)
+        } else {
+          float th, tl;
+          pair_sum2(m, 0.0f, log1pf(__expf(-fabsf(d))), 0.0f, th, tl);
+          pair_sum2(th, tl, -ln2_h, -ln2_l, th, tl);
+          pair_sum2(th, tl, off_h, off_l, mh, ml);
+        }
+      }
+      // v_dZ = (lX_prev + lt) + lmid, v_c = ((lX2_prev + ltT) - lX_cur) + lmid,
+      // v_t2 = (lX2_prev + lt2) + 2 lmid
+      float vch = -INFINITY, vcl = 0.0f;
+      dzh[j] = -INFINITY; dzl[j] = 0.0f; t2h[j] = -INFINITY; t2l[j] = 0.0f;
+      if (valid && mh > -INFINITY) {
+        float qh, ql;
+        pair_sum2(xph, xpl, cp[2], cp[3], qh, ql);
+        pair_sum2(qh, ql, mh, ml, dzh[j], dzl[j]);
+        pair_sum2(x2ph, x2pl, cp[8], cp[9], qh, ql);
+        pair_sum2(qh, ql, -xch[j], -xcl[j], qh, ql);
+        pair_sum2(qh, ql, mh, ml, vch, vcl);
+        pair_sum2(x2ph, x2pl, cp[6], cp[7], qh, ql);
+        pair_sum2(qh, ql, 2.0f * mh, 2.0f * ml, t2h[j], t2l[j]);
+      }
+      cj[j] = fs_term(vch, vcl);
+    }
+    // this thread's exclusive sums of c (cex[j]: elements before j), then A_{k-1} = A_0 + the
+    // CTA's exclusive prefix of c + cex[j]
+    FS cex[K];
+    cex[0] = fs_zero();
+#pragma unroll
+    for (int j = 1; j < K; ++j) cex[j] = fs_sum(cex[j - 1], cj[j - 1]);
+    const FS crun = fs_sum(cex[K - 1], cj[K - 1]);
+    FS cin, cthr, ctot;
+    cta_scan_fs(crun, cin, cthr, ctot, fsm);
+    const FS At = fs_sum(A0, cthr);
+    // with OUT_LZ, the running Z needs the CTA's prefix of dZ as well
+    FS tdZ[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) tdZ[j] = fs_term(dzh[j], dzl[j]);
+    FS zthr = fs_zero(), ztot = fs_zero();
+    if (OUT_LZ) {
+      FS zrun = fs_zero();
+#pragma unroll
+      for (int j = 0; j < K; ++j) zrun = fs_sum(zrun, tdZ[j]);
+      FS zin;
+      cta_scan_fs(zrun, zin, zthr, ztot, fsm);
+      zthr = fs_sum(Z0, zthr);
+    }
+    // (C) per element, independently: the outputs and the terms of this thread's sums, which
+    // are added as a tree
+    FS sZ[K], sZ2[K], sdZ2[K], sP[K], sQ[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const long long k = k0 + j;
+      const bool valid = k < M;
+      if (valid) {
+        if (out_lX) out_lX[k] = pair_to_double(xch[j], xcl[j]);
+        if (out_ldZ) out_ldZ[k] = pair_to_double(dzh[j], dzl[j]);
+      }
+      const FS tt2 = fs_term(t2h[j], t2l[j]);
+      // 2 dZ_k A_{k-1}, a product of pair-scaled values (no log and exp round trip)
+      FS t1 = fs_mul(tdZ[j], fs_sum(At, cex[j]));
+      t1.e += 1;
+      sZ[j] = tdZ[j];
+      sZ2[j] = fs_sum(t1, tt2);
+      sdZ2[j] = tt2;
+      sP[j] = fs_zero();
+      sQ[j] = fs_zero();
+      if (h_out && valid) {
+        const FS tl = fs_scale(tdZ[j], fabsf(Lk[j]));
+        if (Lk[j] >= 0.0f) sP[j] = tl;
+        else sQ[j] = tl;
+      }
+      // the chunk's last element carries its log dZ and L to the next call
+      if (k == (M - base < CH ? M : base + CH) - 1) {
+        sm.last_ldZ = pair_to_double(dzh[j], dzl[j]);
+        sm.last_L = Lk[j];
       }
     }
-    // v_dZ = (lX_prev + lt) + lmid, v_c = ((lX2_prev + ltT) - lX_cur) + lmid,
-    // v_t2 = (lX2_prev + lt2) + 2 lmid
-    float dzh = -INFINITY, dzl = 0.0f, vch = -INFINITY, vcl = 0.0f, t2h = -INFINITY, t2l = 0.0f;
-    if (valid && mh > -INFINITY) {
-      float ah, al;
-      pair_sum2(xph, xpl, cp[2], cp[3], ah, al);
-      pair_sum2(ah, al, mh, ml, dzh, dzl);
-      pair_sum2(x2ph, x2pl, cp[8], cp[9], ah, al);
-      pair_sum2(ah, al, -xch, -xcl, ah, al);
-      pair_sum2(ah, al, mh, ml, vch, vcl);
-      pair_sum2(x2ph, x2pl, cp[6], cp[7], ah, al);
-      pair_sum2(ah, al, 2.0f * mh, 2.0f * ml, t2h, t2l);
-    }
-    // A_{k-1} = A_0 + the exclusive prefix of c
-    FS cin, cex, ctot;
-    cta_scan_fs(fs_term(vch, vcl), cin, cex, ctot, fsm);
-    const FS Ap = fs_sum(A0, cex);
-    float lah, lal;
-    fs_log_pair(Ap, lah, lal);
-    float t1h = -INFINITY, t1l = 0.0f;
-    if (valid && dzh > -INFINITY && lah > -INFINITY) {
-      pair_sum2(dzh, dzl, ln2_h, ln2_l, t1h, t1l);
-      pair_sum2(t1h, t1l, lah, lal, t1h, t1l);
-    }
-    if (valid) {
-      if (out_lX) out_lX[k] = sm.carry_lX + ((double)sTh + (double)sTl);
-      if (out_ldZ) out_ldZ[k] = dzh > -INFINITY ? (double)dzh + (double)dzl : -INFINITY;
-    }
-    const FS tdZ = fs_term(dzh, dzl), tt2 = fs_term(t2h, t2l);
-    FS ztot = fs_zero();
     if (OUT_LZ) {
-      FS zin, zex;
-      cta_scan_fs(tdZ, zin, zex, ztot, fsm);
-      if (valid && out_lZ) out_lZ[k] = fs_log_d(fs_sum(Z0, zin));
-      Z0 = fs_sum(Z0, ztot);
-    } else {
-      pZ = fs_sum(pZ, tdZ);
+#pragma unroll
+      for (int j = 0; j < K; ++j) {
+        zthr = fs_sum(zthr, tdZ[j]);
+        if (k0 + j < M && out_lZ) out_lZ[k0 + j] = fs_log_d(zthr);
+      }
     }
-    pZ2 = fs_sum(pZ2, fs_sum(fs_term(t1h, t1l), tt2));
-    pdZ2 = fs_sum(pdZ2, tt2);
-    // carries into the next chunk: pairs in every thread, FP64 in thread 0
-    pair_sum2(lxh, lxl, tot.x, tot.y, lxh, lxl);
-    pair_sum2(lx2h, lx2l, tot.z, tot.w, lx2h, lx2l);
+#pragma unroll
+    for (int w = 1; w < K; w <<= 1) {
+#pragma unroll
+      for (int j = 0; j + w < K; j += 2 * w) {
+        sZ[j] = fs_sum(sZ[j], sZ[j + w]);
+        sZ2[j] = fs_sum(sZ2[j], sZ2[j + w]);
+        sdZ2[j] = fs_sum(sdZ2[j], sdZ2[j + w]);
+        if (h_out) {
+          sP[j] = fs_sum(sP[j], sP[j + w]);
+          sQ[j] = fs_sum(sQ[j], sQ[j + w]);
+        }
+      }
+    }
+    if (!OUT_LZ) pZ = fs_sum(pZ, sZ[0]);
+    pZ2 = fs_sum(pZ2, sZ2[0]);
+    pdZ2 = fs_sum(pdZ2, sdZ2[0]);
+    if (h_out) {
+      pHP = fs_sum(pHP, sP[0]);
+      pHQ = fs_sum(pHQ, sQ[0]);
+    }
+    // carries into the next chunk: FP64 in thread 0, re-read as pairs by every thread
     A0 = fs_sum(A0, ctot);
-    const long long last = (M - base < T ? M - base : T) - 1;
-    if (tid == last) {
-      sm.last_ldZ = dzh > -INFINITY ? (double)dzh + (double)dzl : -INFINITY;
-      sm.last_L = Lk;
-    }
+    if (OUT_LZ) Z0 = fs_sum(Z0, ztot);
     __syncthreads();  // every thread has read sm.carry_lX for this chunk
     if (tid == 0) {
       acc.lX += (double)tot.x + (double)tot.y;
@@ -623,10 +779,13 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
       acc.A = ss_sum(acc.A, ss_from_fs(ctot));
       if (OUT_LZ) acc.Z = ss_sum(acc.Z, ss_from_fs(ztot));
       sm.carry_lX = acc.lX;
+      sm.carry_lX2 = acc.lX2;
     }
+    __syncthreads();
     acc.ldZ_last = sm.last_ldZ;
     acc.Lprev = sm.last_L;
-    __syncthreads();
+    pair_of(sm.carry_lX, lxh, lxl);
+    pair_of(sm.carry_lX2, lx2h, lx2l);
   }
   // CTA reduction of the partial sums (butterfly in each warp, then across warps in order)
   const int lane = tid & 31, w = tid >> 5, nw = T >> 5;
@@ -635,19 +794,36 @@ __device__ void evidence_scan_cta(EvAcc &acc, const float *__restrict__ L, long 
     pZ = fs_sum(pZ, shfl_xor_fs(pZ, o));
     pZ2 = fs_sum(pZ2, shfl_xor_fs(pZ2, o));
     pdZ2 = fs_sum(pdZ2, shfl_xor_fs(pdZ2, o));
+    if (h_out) {
+      pHP = fs_sum(pHP, shfl_xor_fs(pHP, o));
+      pHQ = fs_sum(pHQ, shfl_xor_fs(pHQ, o));
+    }
   }
   if (lane == 0) {
     fsm.red[0][w] = pZ;
     fsm.red[1][w] = pZ2;
     fsm.red[2][w] = pdZ2;
+    fsm.red[3][w] = pHP;
+    fsm.red[4][w] = pHQ;
   }
   __syncthreads();
   if (tid == 0) {
-    FS rZ = fs_zero(), rZ2 = fs_zero(), rdZ2 = fs_zero();
+    FS rZ = fs_zero(), rZ2 = fs_zero(), rdZ2 = fs_zero(), rP = fs_zero(), rQ = fs_zero();
     for (int q = 0; q < nw; ++q) {
       rZ = fs_sum(rZ, fsm.red[0][q]);
       rZ2 = fs_sum(rZ2, fsm.red[1][q]);
       rdZ2 = fs_sum(rdZ2, fsm.red[2][q]);
+      if (h_out) {
+        rP = fs_sum(rP, fsm.red[3][q]);
+        rQ = fs_sum(rQ, fsm.red[4][q]);
+      }
+    }
+    if (h_out) {
+      // each sum over this scan's own sum of dZ (FP64 ratio of the two scaled sums)
+      const ScaledSum z = ss_from_fs(rZ);
+      const ScaledSum hs[2] = {ss_from_fs(rP), ss_from_fs(rQ)};
+      for (int q = 0; q < 2; ++q)
+        h_out[q] = (z.q > 0.0 && hs[q].q > 0.0) ? (hs[q].q / z.q) * pow2i(hs[q].e - z.e) : 0.0;
     }
     acc.Z = ss_sum(acc.Z, ss_from_fs(rZ));
     acc.Z2 = ss_sum(acc.Z2, ss_from_fs(rZ2));

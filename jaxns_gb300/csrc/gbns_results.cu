@@ -31,27 +31,38 @@ struct RadixSmem {
 // result is in a (an even number of passes).  blockDim.x must be 1024.
 __device__ void cta_radix_keys(long long M, unsigned long long *a, unsigned long long *tmp, RadixSmem &sm);
 
-// Stable ascending sort of the N+1 node keys (by their upper 32 bits).  Result in a (perm
-// in the low 32 bits).  a, tmp: [N+1] scratch.  blockDim.x must be 1024.
-__device__ unsigned long long *cta_sort_nodes(const float *L, long long N, unsigned long long *a,
-                                              unsigned long long *tmp, RadixSmem &sm) {
+// Stable ascending sort of the N+1 node keys (by their upper 32 bits).  Returns nullptr when
+// the nodes are already in order (the usual case: dead points arrive sorted, so the
+// permutation is the identity and nothing is written), else the sorted keys in a (perm in the
+// low 32 bits).  a, tmp: [N+1] scratch.  blockDim.x must be 1024.
+__device__ const unsigned long long *cta_sort_nodes(const float *L, long long N, unsigned long long *a,
+                                                    unsigned long long *tmp, RadixSmem &sm) {
   const long long M = N + 1;
   const int tid = threadIdx.x;
   if (tid == 0) sm.flag = 1;
-  for (int q = tid; q < 4 * 256; q += blockDim.x) (&sm.hist[0][0])[q] = 0;
   __syncthreads();
   int sorted = 1;
+  // four strided elements per thread per pass, their loads in flight together
+  for (long long i0 = tid + 1; i0 < M; i0 += 4ll * blockDim.x) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const long long i = i0 + (long long)j * blockDim.x;
+      if (i < M && (node_key(L, i - 1) >> 32) > (node_key(L, i) >> 32)) sorted = 0;
+    }
+  }
+  if (!sorted) sm.flag = 0;
+  __syncthreads();
+  if (sm.flag) return nullptr;
+  for (int q = tid; q < 4 * 256; q += blockDim.x) (&sm.hist[0][0])[q] = 0;
+  __syncthreads();
   for (long long i = tid; i < M; i += blockDim.x) {
     const unsigned long long k = node_key(L, i);
     a[i] = k;
-    if (i > 0 && (node_key(L, i - 1) >> 32) > (k >> 32)) sorted = 0;
     const uint32_t key = (uint32_t)(k >> 32);
 #pragma unroll
     for (int d = 0; d < 4; ++d) atomicAdd(&sm.hist[d][(key >> (8 * d)) & 255], 1);
   }
-  if (!sorted) sm.flag = 0;
   __syncthreads();
-  if (sm.flag) return a;
   cta_radix_keys(M, a, tmp, sm);
   return a;
 }
@@ -103,44 +114,80 @@ __device__ void cta_radix_keys(long long M, unsigned long long *a, unsigned long
   }
 }
 
-// count_crossed_edges on one sample set (static variant).  perm: sorted node keys.
-// deg: [N+1] scratch.  Outputs [N].
+// count_crossed_edges on one sample set (static variant).  perm: sorted node keys, or nullptr
+// for nodes already in order.  deg: [N+1] scratch.  Outputs [N]; visit(pos, k) is called once
+// for every sorted position pos < N with its sample index k (the caller's gather).
+struct NoVisit {
+  __device__ void operator()(long long, int) const {}
+};
+
+template <typename Visit>
 __device__ void cta_count_edges(const int *sender, long long N, const unsigned long long *perm, int *deg,
-                                int *samples_indices, int *num_live, RadixSmem &sm) {
+                                int *samples_indices, int *num_live, RadixSmem &sm, Visit visit) {
+  constexpr int K = 4;  // elements per thread per pass: their loads are in flight together
   const long long M = N + 1;
-  for (long long i = threadIdx.x; i < M; i += blockDim.x) deg[i] = 0;
+  const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, w = tid >> 5, nw = T >> 5;
+  for (long long i = tid; i < M; i += T) deg[i] = 0;
   __syncthreads();
   // out_degree.at[max(sender, 0)].add(1) (tree_structure.py:82-84); like jax's scatter, an
   // update outside [0, N] is dropped, so a bad sender never writes past the scratch
-  for (long long i = threadIdx.x; i < N; i += blockDim.x) {
-    const int sd = max(sender[i], 0);
-    if ((long long)sd <= N) atomicAdd(&deg[sd], 1);
+  for (long long i0 = tid; i0 < N; i0 += (long long)K * T) {
+    int sd[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const long long i = i0 + (long long)j * T;
+      sd[j] = i < N ? max(sender[i], 0) : -1;
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (sd[j] >= 0 && (long long)sd[j] <= N) atomicAdd(&deg[sd[j]], 1);
   }
-  __syncthreads();
-  if (threadIdx.x == 0) sm.carry = 1;
+  if (tid == 0) sm.carry = 1;
   __syncthreads();
   __shared__ long long wsum[32];
-  for (long long t0 = 0; t0 < M; t0 += blockDim.x) {
-    const long long i = t0 + threadIdx.x;
-    const int node = i < M ? (int)(perm[i] & 0xffffffffu) : 0;
-    long long v = i < M ? (long long)deg[node] - 1 : 0;
-    v = warp_incl_scan(v);
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    if (lane == 31) wsum[w] = v;
+  // crossed-edge scan over the sorted positions, K consecutive positions per thread
+  for (long long base = 0; base < M; base += (long long)K * T) {
+    const long long i0 = base + (long long)tid * K;
+    int node[K], v[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const long long i = i0 + j;
+      node[j] = i < M ? (perm ? (int)(perm[i] & 0xffffffffu) : (int)i) : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < K; ++j) v[j] = i0 + j < M ? deg[node[j]] - 1 : 0;
+    // the caller's gather has no part in the scan: its loads go out before the barriers
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const long long i = i0 + j;
+      if (i >= 1 && i < M) {
+        samples_indices[i - 1] = node[j] - 1;
+        visit(i - 1, node[j] - 1);
+      }
+    }
+    int loc[K];
+    int run = 0;
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      run += v[j];
+      loc[j] = run;
+    }
+    const long long tsum = run;
+    const long long incl = warp_incl_scan(tsum);
+    if (lane == 31) wsum[w] = incl;
     __syncthreads();
     if (w == 0) {
-      long long x = wsum[lane];
+      long long x = lane < nw ? wsum[lane] : 0;
       x = warp_incl_scan(x);
       wsum[lane] = x;
     }
     __syncthreads();
-    const long long crossed = sm.carry + v + (w > 0 ? wsum[w - 1] : 0);
-    if (i < N) {
-      num_live[i] = (int)crossed;
-    }
-    if (i >= 1 && i < M) samples_indices[i - 1] = node - 1;
+    const long long excl = sm.carry + (incl - tsum) + (w > 0 ? wsum[w - 1] : 0);
+#pragma unroll
+    for (int j = 0; j < K; ++j)
+      if (i0 + j < N) num_live[i0 + j] = (int)(excl + loc[j]);
     __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) sm.carry = crossed;
+    if (tid == T - 1) sm.carry = excl + loc[K - 1];  // positions past M add nothing
     __syncthreads();
   }
 }
@@ -151,8 +198,8 @@ __global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const f
                                                       int *samples_indices, int *num_live,
                                                       unsigned long long *scratch, int *deg) {
   __shared__ RadixSmem sm;
-  unsigned long long *perm = cta_sort_nodes(L, N, scratch, scratch + (N + 1), sm);
-  cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm);
+  const unsigned long long *perm = cta_sort_nodes(L, N, scratch, scratch + (N + 1), sm);
+  cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm, NoVisit{});
 }
 
 // ---- count_crossed_edges of one large sample set over many CTAs ---------------------------
@@ -266,31 +313,39 @@ __global__ void __launch_bounds__(1024) k_ce_chunk_out(long long N, const unsign
   }
 }
 
+// Evidence scans over sample sets: threads per CTA and consecutive samples per thread.
+constexpr int RESULTS_K = 4;
+constexpr int RESULTS_EV_THREADS = 512;
+
 // compute_evidence_stats (internals/shrinkage_statistics.py:131-157) of one sample set on one
 // CTA: the final register and the per-sample log X, log dZ and log Z, FP64 (gbns_evidence_stats).
 template <bool OUT_LZ>
-__global__ void __launch_bounds__(1024) k_evidence_stats(const float *L, const int *nl, long long N, const double *ncoef,
-                                                         int nmax, gbns_evcalc *fin, double *lX, double *ldZ,
-                                                         double *lZ) {
+__global__ void __launch_bounds__(RESULTS_EV_THREADS)
+    k_evidence_stats(const float *L, const int *nl, long long N, const double *ncoef, int nmax, gbns_evcalc *fin,
+                     double *lX, double *ldZ, double *lZ) {
   __shared__ EvScanSmem esm;
   gbns_evcalc e;
   e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
   e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
   EvAcc acc = evacc_from(e);
-  evidence_scan_cta<OUT_LZ>(acc, L, N, 0, 0, nl, ncoef, nmax, lX, ldZ, lZ, 0.0, nullptr, esm);
+  evidence_scan_cta<OUT_LZ, RESULTS_K>(acc, L, N, 0, 0, nl, ncoef, nmax, lX, ldZ, lZ, 0.0, nullptr, esm);
   if (threadIdx.x == 0) *fin = evacc_to(acc, N > 0 ? (double)L[N - 1] : -INFINITY);
 }
 
 // ------------------------------------------------------------ results ----
 
-// _to_results (sharded_static.py:652-773) for every run of a batch, one CTA per run: tree count
-// of the run's store, gather in sorted order, FP64 evidence per sample, log Z mean and
-// uncertainty with the phantom correction, ESS, H, efficiency.
-__global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_bufs res) {
+// _to_results (sharded_static.py:652-773) for every run of a batch, one CTA per run, in two
+// launches.  k_results_tree: tree count of the run's store and the gather in sorted order
+// (1024 threads: the radix sort and the crossed-edge scan are latency-bound passes).
+// k_results_ev: FP64 evidence per sample, log Z mean and uncertainty with the phantom
+// correction, ESS, H, efficiency (512 threads of RESULTS_K consecutive samples each: the
+// evidence scan is instruction-bound and runs its prefixes per thread; 256 x 8 and 1024 x 1
+// were slower, 256 x 8 by 1.3x: too few warps to hide the per-thread chains).
+
+__global__ void __launch_bounds__(1024) k_results_tree(gbns_batch b, gbns_results_bufs res, int deg_smem_cap) {
+  extern __shared__ int sdeg[];  // the out-degrees of a run of up to deg_smem_cap - 1 samples
   __shared__ RadixSmem sm;
-  __shared__ double dred[32];
   __shared__ long long lred[32];
-  __shared__ double s_lz[4];
   const int r = blockIdx.x;
   const gbns_run_desc &rd = b.runs[r];
   const gbns_run_state &st = b.state[r];
@@ -298,25 +353,27 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
   const long long so = rd.store_off;
   const int D = rd.ucols;  // 32-bit words of U per sample
   unsigned long long *scratch = (unsigned long long *)res.scratch_ll + 2 * (so + r);
-  int *deg = res.scratch_i + (so + r);
+  int *deg_g = res.scratch_i + (so + r);
+  int *deg = N + 1 <= deg_smem_cap ? sdeg : deg_g;  // shared-memory atomics and reads when they fit
   int *si = res.samples_indices + so;
   int *nl = res.num_live_points + so;
   const unsigned long long *perm = cta_sort_nodes(b.store_L + so, N, scratch, scratch + (N + 1), sm);
-  cta_count_edges(b.store_S + so, N, perm, deg, si, nl, sm);
-  __syncthreads();
-  // gather in sorted order
+  // the gather in sorted order rides on the crossed-edge scan's pass over the sorted positions
   double *Ls = res.log_L_samples + so;
   const double off = rd.log_L_offset;
   int *Es = res.nevals_sorted + so;
+  const float *Lst = b.store_L + so;
+  const int *Est = b.store_E + so;
+  const uint8_t *Pst = b.store_P + so;
   long long ev_sum = 0, ph_sum = 0;
-  for (long long i = threadIdx.x; i < N; i += blockDim.x) {
-    const int k = si[i];
-    Ls[i] = (double)b.store_L[so + k] + off;
-    const int e = b.store_E[so + k];
-    Es[i] = e;
+  cta_count_edges(b.store_S + so, N, perm, deg, si, nl, sm, [&](long long pos, int k) {
+    Ls[pos] = (double)Lst[k] + off;
+    const int e = Est[k];
+    Es[pos] = e;
     ev_sum += e;
-    ph_sum += b.store_P[so + i];
-  }
+    ph_sum += Pst[pos];
+  });
+  __syncthreads();
   if (res.U_sorted && rd.ustore_off >= 0 && b.store_U) {
     float *Us = res.U_sorted + rd.ustore_off;
     const float *Ust = b.store_U + rd.ustore_off;
@@ -327,16 +384,38 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
   }
   const long long total_evals = cta_sum_ll(ev_sum, lred);
   const long long total_phantom = cta_sum_ll(ph_sum, lred);
-  __syncthreads();
-  // evidence statistics (CTA-wide FP64 scan)
+  if (threadIdx.x == 0) {
+    double *sc = res.scalars + 8 * (size_t)r;
+    sc[4] = (double)N;
+    sc[5] = (double)total_phantom;
+    sc[6] = (double)total_evals;
+    deg_g[0] = perm != nullptr;  // the degree scratch is spent: its first word tells the evidence pass to gather
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(RESULTS_EV_THREADS) k_results_ev(gbns_batch b, gbns_results_bufs res) {
+  __shared__ double s_lz[4];
+  __shared__ double s_h[2];
+  __shared__ double dred[32];
+  __shared__ EvScanSmem esm;
+  const int r = blockIdx.x;
+  const gbns_run_desc &rd = b.runs[r];
+  const gbns_run_state &st = b.state[r];
+  const long long N = st.num_samples < rd.cap ? st.num_samples : rd.cap;
+  const long long so = rd.store_off;
+  const int *si = res.samples_indices + so;
+  const int *nl = res.num_live_points + so;
+  const bool gathered = res.scratch_i[so + r] != 0;
+  const double off = rd.log_L_offset;
   double *lX = res.log_X_mean + so, *ldp = res.log_dp_mean + so;
   {
-    __shared__ EvScanSmem esm;
     gbns_evcalc e;
     e.log_L = -INFINITY; e.log_X_mean = 0.0; e.log_X2_mean = 0.0; e.log_Z_mean = -INFINITY;
     e.log_ZX_mean = -INFINITY; e.log_Z2_mean = -INFINITY; e.log_dZ_mean = -INFINITY; e.log_dZ2_mean = -INFINITY;
     EvAcc acc = evacc_from(e);
-    evidence_scan_cta<false>(acc, b.store_L + so, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr, off, si, esm);
+    evidence_scan_cta<false, K>(acc, b.store_L + so, N, 0, 0, nl, b.ncoef, b.ncoef_n, lX, ldp, nullptr, off,
+                                gathered ? si : nullptr, esm, s_h);
     if (threadIdx.x == 0) {
       const gbns_evcalc f = evacc_to(acc, 0.0);
       s_lz[0] = f.log_Z_mean;
@@ -346,35 +425,46 @@ __global__ void __launch_bounds__(1024) k_results(gbns_batch b, gbns_results_buf
   }
   __syncthreads();
   // normalise_log_space(log_dZ_mean) and H (sharded_static.py:726-737): the normaliser
-  // logsumexp(log_dZ_mean) is log sum dZ = log Z, which the scan has just accumulated
+  // logsumexp(log_dZ_mean) is log sum dZ = log Z, which the scan has just accumulated, and the
+  // scan has formed the dZ-weighted mean of L that H takes
   const double lZ = s_lz[0], lZ2 = s_lz[1], ldZ2 = s_lz[2];
   const double norm = lZ;
   const double mu = 2.0 * lZ - 0.5 * lZ2;
-  double h1 = 0.0, h2 = 0.0;
-  for (long long i = threadIdx.x; i < N; i += blockDim.x) {
-    const double v = (norm > -INFINITY) ? ldp[i] - norm : -INFINITY;
-    ldp[i] = v;
-    const double w = (v > -INFINITY) ? (double)__expf((float)v) : 0.0;
-    h1 += w * ((v > -INFINITY) ? (double)Ls[i] : 0.0);
-    h2 += w * (-lX[i]);
+  for (long long i0 = threadIdx.x; i0 < N; i0 += 4ll * blockDim.x) {
+    double v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const long long i = i0 + (long long)j * blockDim.x;
+      v[j] = i < N ? ldp[i] : 0.0;
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const long long i = i0 + (long long)j * blockDim.x;
+      if (i < N) ldp[i] = (norm > -INFINITY) ? v[j] - norm : -INFINITY;
+    }
   }
-  h1 = cta_sum_d(h1, dred);
-  h2 = cta_sum_d(h2, dred);
+  const double h1 = (s_h[0] - s_h[1]) + off;
+  const double H_inst = -(h1 - mu);
+  // the stable form E[-log X] only where the direct one is not finite (every thread takes the
+  // same branch)
+  double h2 = 0.0;
+  if (!isfinite(H_inst)) {
+    __syncthreads();  // the normalised log dp of every sample is written
+    for (long long i = threadIdx.x; i < N; i += blockDim.x) h2 += ldp[i] > -INFINITY ? exp(ldp[i]) * -lX[i] : 0.0;
+    h2 = cta_sum_d(h2, dred);
+  }
   if (threadIdx.x == 0) {
+    double *sc = res.scalars + 8 * (size_t)r;
+    const double total_phantom = sc[5], total_evals = sc[6];
     double var = lZ2 - 2.0 * lZ;
     var = (var != var) ? var : fmax(var, 2.220446049250313e-16);
-    const double pf = (double)total_phantom / (double)N;
+    const double pf = total_phantom / (double)N;
     const double k = pf / (1.0 - pf);
-    double *sc = res.scalars + 8 * (size_t)r;
     sc[0] = mu;
     sc[1] = sqrt(var) * sqrt(1.0 + k);
     sc[2] = exp(2.0 * lZ - ldZ2) / (1.0 + k);
-    const double H_inst = -(h1 - mu);
     sc[3] = isfinite(H_inst) ? H_inst : -h2;
-    sc[4] = (double)N;
-    sc[5] = (double)total_phantom;
-    sc[6] = (double)total_evals;
-    sc[7] = log((double)N) - log((double)total_evals);
+    sc[7] = log((double)N) - log(total_evals);
   }
 }
 
@@ -573,7 +663,18 @@ cudaError_t launch_rng(int mode, const uint32_t *key, const uint32_t *counts, vo
 }
 
 cudaError_t launch_results(const gbns_batch &b, const gbns_results_bufs &res, cudaStream_t stream) {
-  k_results<<<b.num_runs, 1024, 0, stream>>>(b, res);
+  // out-degrees in dynamic shared memory beside the kernel's static shared memory
+  int dev = 0, optin = 0;
+  cudaError_t e;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev)) != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  if ((e = cudaFuncGetAttributes(&fa, k_results_tree)) != cudaSuccess) return e;
+  const int dyn = ((optin - (int)fa.sharedSizeBytes - 1024) / 16) * 16;
+  if ((e = cudaFuncSetAttribute(k_results_tree, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn)) != cudaSuccess)
+    return e;
+  k_results_tree<<<b.num_runs, 1024, dyn, stream>>>(b, res, dyn / (int)sizeof(int));
+  k_results_ev<RESULTS_K><<<b.num_runs, RESULTS_EV_THREADS, 0, stream>>>(b, res);
   return cudaGetLastError();
 }
 
@@ -607,8 +708,8 @@ cudaError_t launch_count_crossed_edges(const int *sender, const float *L, long l
 
 cudaError_t launch_evidence_stats(const float *L, const int *num_live, long long N, const double *ncoef, int nmax,
                                   gbns_evcalc *final_out, double *lX, double *ldZ, double *lZ, cudaStream_t stream) {
-  if (lZ) k_evidence_stats<true><<<1, 1024, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
-  else k_evidence_stats<false><<<1, 1024, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
+  if (lZ) k_evidence_stats<true><<<1, RESULTS_EV_THREADS, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
+  else k_evidence_stats<false><<<1, RESULTS_EV_THREADS, 0, stream>>>(L, num_live, N, ncoef, nmax, final_out, lX, ldZ, lZ);
   return cudaGetLastError();
 }
 

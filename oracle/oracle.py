@@ -723,3 +723,28 @@ def prior_transform(kind, a, b, log_norm, U, A=None, row_start=None, c=None, log
         U32.ctypes.data_as(fp) if U32 is not None else None, _dp(U64) if U64 is not None else None,
         ctypes.c_long(M), _dp(lL) if lL is not None else None, _dp(X), _dp(out))
     return X, out
+
+
+# ----------------------------------------------------------------------------- results of a store
+
+def results_of_store(sender, log_L, nevals, phantom):
+    """_to_results (sharded_static.py:652-773) of one sample store given as arrays (sender,
+    FP64 log L, evaluation counts, phantom flags, in store order): returns (scalars dict,
+    samples_indices, num_live_points, log_L sorted, log_dp_mean, log_X_mean)."""
+    N = len(log_L)
+    snd = np.ascontiguousarray(sender, np.int64)
+    lL = np.ascontiguousarray(log_L, np.float64)
+    nev = np.ascontiguousarray(nevals, np.int64)
+    ph = np.ascontiguousarray(phantom, np.int32)
+    st = _NSState()
+    st.sender, st.log_L, st.nevals, st.phantom = _lp(snd), _dp(lL), _lp(nev), _ip(ph)
+    st.num_samples = N
+    st.next_sample_idx = N
+    m = _Model()
+    m.D = 1
+    res = _Results()
+    si, nl = np.zeros(max(N, 1), np.int64), np.zeros(max(N, 1), np.int64)
+    ls, dp, lx = (np.zeros(max(N, 1)) for _ in range(3))
+    lib().orc_to_results(ctypes.byref(m), ctypes.byref(st), ctypes.c_long(N), ctypes.byref(res), _lp(si), _lp(nl),
+                         _dp(ls), _dp(dp), _dp(lx), None)
+    return ({f: getattr(res, f) for f, _ in _Results._fields_}, si[:N], nl[:N], ls[:N], dp[:N], lx[:N])
