@@ -31,28 +31,41 @@ struct RadixSmem {
 // result is in a (an even number of passes).  blockDim.x must be 1024.
 __device__ void cta_radix_keys(long long M, unsigned long long *a, unsigned long long *tmp, RadixSmem &sm);
 
-// Stable ascending sort of the N+1 node keys (by their upper 32 bits).  Returns nullptr when
-// the nodes are already in order (the usual case: dead points arrive sorted, so the
-// permutation is the identity and nothing is written), else the sorted keys in a (perm in the
-// low 32 bits).  a, tmp: [N+1] scratch.  blockDim.x must be 1024.
-__device__ const unsigned long long *cta_sort_nodes(const float *L, long long N, unsigned long long *a,
-                                                    unsigned long long *tmp, RadixSmem &sm) {
+// Whether the N+1 node keys are already in order (the usual case: dead points arrive sorted),
+// and, when deg is given (zeroed by the caller), the out-degrees of the sender tree counted in
+// the same pass over the store: out_degree.at[max(sender, 0)].add(1) (tree_structure.py:82-84);
+// like jax's scatter, an update outside [0, N] is dropped, so a bad sender never writes past
+// the scratch.  Four strided elements per thread per pass, their loads in flight together.
+__device__ int cta_nodes_in_order(const float *L, const int *sender, long long N, int *deg, RadixSmem &sm) {
   const long long M = N + 1;
   const int tid = threadIdx.x;
   if (tid == 0) sm.flag = 1;
   __syncthreads();
   int sorted = 1;
-  // four strided elements per thread per pass, their loads in flight together
-  for (long long i0 = tid + 1; i0 < M; i0 += 4ll * blockDim.x) {
+  for (long long i0 = tid; i0 < M; i0 += 4ll * blockDim.x) {
+    int sd[4];
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       const long long i = i0 + (long long)j * blockDim.x;
-      if (i < M && (node_key(L, i - 1) >> 32) > (node_key(L, i) >> 32)) sorted = 0;
+      sd[j] = deg && i < N ? max(sender[i], 0) : -1;
+      if (i >= 1 && i < M && (node_key(L, i - 1) >> 32) > (node_key(L, i) >> 32)) sorted = 0;
     }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (sd[j] >= 0 && (long long)sd[j] <= N) atomicAdd(&deg[sd[j]], 1);
   }
   if (!sorted) sm.flag = 0;
   __syncthreads();
-  if (sm.flag) return nullptr;
+  return sm.flag;
+}
+
+// Stable ascending sort of the N+1 node keys (by their upper 32 bits) of a store that is out
+// of order: the keys in a (perm in the low 32 bits).  a, tmp: [N+1] scratch.  blockDim.x must
+// be 1024.
+__device__ const unsigned long long *cta_sort_node_keys(const float *L, long long N, unsigned long long *a,
+                                                        unsigned long long *tmp, RadixSmem &sm) {
+  const long long M = N + 1;
+  const int tid = threadIdx.x;
   for (int q = tid; q < 4 * 256; q += blockDim.x) (&sm.hist[0][0])[q] = 0;
   __syncthreads();
   for (long long i = tid; i < M; i += blockDim.x) {
@@ -123,15 +136,17 @@ struct NoVisit {
 
 template <typename Visit>
 __device__ void cta_count_edges(const int *sender, long long N, const unsigned long long *perm, int *deg,
-                                int *samples_indices, int *num_live, RadixSmem &sm, Visit visit) {
+                                int *samples_indices, int *num_live, RadixSmem &sm, bool deg_ready, Visit visit) {
   constexpr int K = 4;  // elements per thread per pass: their loads are in flight together
   const long long M = N + 1;
   const int tid = threadIdx.x, T = blockDim.x, lane = tid & 31, w = tid >> 5, nw = T >> 5;
-  for (long long i = tid; i < M; i += T) deg[i] = 0;
-  __syncthreads();
+  if (!deg_ready) {
+    for (long long i = tid; i < M; i += T) deg[i] = 0;
+    __syncthreads();
+  }
   // out_degree.at[max(sender, 0)].add(1) (tree_structure.py:82-84); like jax's scatter, an
   // update outside [0, N] is dropped, so a bad sender never writes past the scratch
-  for (long long i0 = tid; i0 < N; i0 += (long long)K * T) {
+  for (long long i0 = tid; i0 < (deg_ready ? 0 : N); i0 += (long long)K * T) {
     int sd[K];
 #pragma unroll
     for (int j = 0; j < K; ++j) {
@@ -198,8 +213,9 @@ __global__ void __launch_bounds__(1024) k_count_edges(const int *sender, const f
                                                       int *samples_indices, int *num_live,
                                                       unsigned long long *scratch, int *deg) {
   __shared__ RadixSmem sm;
-  const unsigned long long *perm = cta_sort_nodes(L, N, scratch, scratch + (N + 1), sm);
-  cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm, NoVisit{});
+  const unsigned long long *perm =
+      cta_nodes_in_order(L, nullptr, N, nullptr, sm) ? nullptr : cta_sort_node_keys(L, N, scratch, scratch + (N + 1), sm);
+  cta_count_edges(sender, N, perm, deg, samples_indices, num_live, sm, false, NoVisit{});
 }
 
 // ---- count_crossed_edges of one large sample set over many CTAs ---------------------------
@@ -357,7 +373,12 @@ __global__ void __launch_bounds__(1024) k_results_tree(gbns_batch b, gbns_result
   int *deg = N + 1 <= deg_smem_cap ? sdeg : deg_g;  // shared-memory atomics and reads when they fit
   int *si = res.samples_indices + so;
   int *nl = res.num_live_points + so;
-  const unsigned long long *perm = cta_sort_nodes(b.store_L + so, N, scratch, scratch + (N + 1), sm);
+  // out-degrees counted in the pass that checks the order
+  for (long long i = threadIdx.x; i < N + 1; i += blockDim.x) deg[i] = 0;
+  __syncthreads();
+  const unsigned long long *perm = cta_nodes_in_order(b.store_L + so, b.store_S + so, N, deg, sm)
+                                       ? nullptr
+                                       : cta_sort_node_keys(b.store_L + so, N, scratch, scratch + (N + 1), sm);
   // the gather in sorted order rides on the crossed-edge scan's pass over the sorted positions
   double *Ls = res.log_L_samples + so;
   const double off = rd.log_L_offset;
@@ -366,7 +387,7 @@ __global__ void __launch_bounds__(1024) k_results_tree(gbns_batch b, gbns_result
   const int *Est = b.store_E + so;
   const uint8_t *Pst = b.store_P + so;
   long long ev_sum = 0, ph_sum = 0;
-  cta_count_edges(b.store_S + so, N, perm, deg, si, nl, sm, [&](long long pos, int k) {
+  cta_count_edges(b.store_S + so, N, perm, deg, si, nl, sm, true, [&](long long pos, int k) {
     Ls[pos] = (double)Lst[k] + off;
     const int e = Est[k];
     Es[pos] = e;
