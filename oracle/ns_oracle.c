@@ -1250,9 +1250,10 @@ void orc_ns_run_batch(const orc_model *models, const orc_ns_cfg *cfgs, const orc
  * algorithm (uni_slice_sampler.py:114-273, :343-441; bases.py:63-75; random.py:34-84) in
  * exactly the kernels' fp32 operation order, so that each chain's evaluation count,
  * accepted point and log-likelihood can be compared bit for bit.  It differs from the FP64
- * restatement above only in precision and in the order of the two fp32 reductions the
- * kernels perform (sequential per thread, or a butterfly across the 32 lanes of a warp
- * in the warp-cooperative correlated-Gaussian kernel); the RNG stream, the seed choice, the
+ * restatement above only in precision and in the order of the fp32 reductions the kernels
+ * perform (the likelihood's sum of squares, the direction's and the gradient's norms, the
+ * reflection's dot product: sequential per thread, or a butterfly across the 32 lanes of a
+ * warp in the warp-cooperative correlated-Gaussian kernel); the RNG stream, the seed choice, the
  * accept test and the shrink rule are the same.
  * ===================================================================================== */
 
@@ -1408,6 +1409,28 @@ static void o32_grad_u(const orc32_model *m, const float *u, float *g) {
     }
 }
 
+/* sum over the dimensions of p_j q_j in the order of the kernel that runs the chain: one fmaf
+ * chain in dimension order (thread per chain), or, in the warp-cooperative kernel, lane l
+ * holding dimensions l and l + 32 forms fmaf(p_l, q_l, p_{l+32} q_{l+32}) and the 32 lanes
+ * are summed by the xor butterfly.  Used for the gradient's norm and the reflection's dot
+ * product and norm (uni_slice_sampler.py:202-214, :255-269). */
+static float o32_dot_dims(const orc32_model *m, const float *p, const float *q) {
+    int D = m->D;
+    if (m->variant == 0) {
+        float s = 0.0f;
+        for (int j = 0; j < D; ++j) s = fmaf(p[j], q[j], s);
+        return s;
+    }
+    float a[32];
+    for (int l = 0; l < 32; ++l) {
+        float p0 = l < D ? p[l] : 0.0f, q0 = l < D ? q[l] : 0.0f;
+        int hi = m->variant > 32 && l + 32 < D;
+        float p1 = hi ? p[l + 32] : 0.0f, q1 = hi ? q[l + 32] : 0.0f;
+        a[l] = fmaf(p0, q0, p1 * q1);
+    }
+    return o32_butterfly(a);
+}
+
 /* _sample_direction (uni_slice_sampler.py:23-38): D normals, normalised by one reciprocal of
  * the norm (sum of squares sequential per thread, or the warp kernel's butterfly). */
 static void o32_direction(const orc32_model *m, okey k, float *d) {
@@ -1478,11 +1501,10 @@ void orc32_slice_chain(const orc32_model *m, const orc_slice_cfg *cfg, uint32_t 
         int climb = 0;
         if (cfg->gradient_slice) {
             /* gradient_slice (uni_slice_sampler.py:202-214) */
-            float g[128], gg = 0.0f;
+            float g[128];
             o32_grad_u(m, u0, g);
             ++total;
-            for (int q = 0; q < D; ++q) gg = fmaf(g[q], g[q], gg);
-            float gn = sqrtf(gg);
+            float gn = sqrtf(o32_dot_dims(m, g, g));
             if (gn != 0.0f && isfinite(gn)) {
                 climb = 1;
                 for (int q = 0; q < D; ++q) d[q] = g[q] / gn;
@@ -1531,20 +1553,17 @@ void orc32_slice_chain(const orc32_model *m, const orc_slice_cfg *cfg, uint32_t 
             /* Householder reflection at the accepted point (uni_slice_sampler.py:255-269) */
             ++total;
             if (j + 1 < S) {
-                float g[128], gg = 0.0f;
+                float g[128];
                 o32_grad_u(m, u0, g);
-                for (int q = 0; q < D; ++q) gg = fmaf(g[q], g[q], gg);
-                float gn = sqrtf(gg);
+                float gn = sqrtf(o32_dot_dims(m, g, g));
                 if (!(gn >= 1e-10f) || isinf(gn)) {
                     o32_direction(m, key_fold(after, 0), d);
                 } else {
-                    float dot = 0.0f, dd = 0.0f;
-                    for (int q = 0; q < D; ++q) dot = fmaf(d[q], g[q] / gn, dot);
-                    for (int q = 0; q < D; ++q) {
-                        d[q] = fmaf(-2.0f * dot, g[q] / gn, d[q]);
-                        dd = fmaf(d[q], d[q], dd);
-                    }
-                    float dn = sqrtf(dd);
+                    float gu[128];
+                    for (int q = 0; q < D; ++q) gu[q] = g[q] / gn;
+                    float dot = o32_dot_dims(m, d, gu);
+                    for (int q = 0; q < D; ++q) d[q] = fmaf(-2.0f * dot, gu[q], d[q]);
+                    float dn = sqrtf(o32_dot_dims(m, d, d));
                     for (int q = 0; q < D; ++q) d[q] = d[q] / dn;
                 }
             }

@@ -659,8 +659,6 @@ def slice_shell32(model: Model32, key, L_star, live_U, live_logL, num_chains, nu
     D = model.D
     live_U = np.ascontiguousarray(live_U, np.float32)
     live_logL = np.ascontiguousarray(live_logL, np.float32)
-    if (gradient_guided or gradient_slice) and model.variant != 0:
-        raise NotImplementedError("the fp32 mode models the gradient options of the thread-per-chain kernel")
     cfg = _SliceCfg(num_slices, num_phantom, int(midpoint_shrink), int(gradient_guided), int(gradient_slice))
     U = np.zeros((num_chains, D), np.float32)
     L = np.zeros(num_chains, np.float32)

@@ -240,11 +240,12 @@ def test_gradient_options_chain_parity(gpu_lib, oracle_mod, D, n, S, guided, cli
     """UniDimSliceSampler's gradient options: gradient_guided (the direction of the next slice
     is the reflection about the U-space gradient at the accepted point, uni_slice_sampler.py:
     255-269) and gradient_slice (each slice runs along the normalised gradient at its seed,
-    t >= 0, :202-214), one extra evaluation per gradient.  One thread per chain (D <= 16):
-    every chain bit for bit the fp32 kernel-arithmetic oracle.  Warp-cooperative kernel
-    (D > 16, its gradient sums over lanes): against the FP64 restatement, where each
-    direction depends on the previous accepted point, so fp32-vs-FP64 differences carry from
-    slice to slice; the bar applies to a few slices."""
+    t >= 0, :202-214), one extra evaluation per gradient.  Every chain bit for bit the fp32
+    kernel-arithmetic oracle, for the thread-per-chain kernel (D <= 16) and the
+    warp-cooperative one (D > 16, whose gradient norm and reflection sums run over lanes).
+    Against the FP64 restatement each direction depends on the previous accepted point, so
+    fp32-vs-FP64 differences carry from slice to slice: reported for the warp kernel, not a
+    pass criterion."""
     from jaxns_gb300.engine import NSBatch
     key = oracle_mod.PRNGKey(50 + D)
     spec, (mu, cov) = _spec(D, n, S, key, seed=D)
@@ -260,8 +261,8 @@ def test_gradient_options_chain_parity(gpu_lib, oracle_mod, D, n, S, guided, cli
     torch.cuda.synchronize()
     E_g = b.new_E[:s].cpu().numpy()
     assert np.all(E_g >= S * (1 + int(guided) + int(climb)))  # a proposal and each gradient per slice
+    assert_shell_exact(oracle_mod, b, 0, Ls_raw, skey)
     if D <= 16:
-        assert_shell_exact(oracle_mod, b, 0, Ls_raw, skey)
         return
     om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
     U_o, L_o, E_o = oracle_mod.slice_shell(om, skey, Lstar, live["U"].cpu().double().numpy(),
@@ -269,7 +270,7 @@ def test_gradient_options_chain_parity(gpu_lib, oracle_mod, D, n, S, guided, cli
                                            gradient_slice=climb)
     U_g = b.new_U[:s * D].view(s, D).cpu().numpy()
     same = (E_g == E_o) & np.all(np.abs(U_g - U_o) < 2e-4, axis=1)
-    assert same.mean() >= 0.9, f"chain parity {same.mean():.3f}"
+    print(f"D={D}: warp-kernel chains equal to the FP64 restatement: {same.mean():.3f}")
 
 
 def test_gradient_slice_shells_exact(gpu_lib, oracle_mod):
