@@ -139,19 +139,24 @@ def test_init_live_points_match_oracle(gpu_lib, oracle_mod):
 
 @pytest.mark.parametrize("D,n,S,K,normal", [(2, 64, 8, 0, False), (8, 512, 32, 0, False), (10, 200, 50, 0, False),
                                              (24, 128, 24, 0, False), (64, 96, 64, 0, False), (5, 128, 20, 3, False),
-                                             (12, 256, 24, 0, True), (40, 96, 40, 2, True)])
+                                             (12, 256, 24, 0, True), (40, 96, 40, 2, True), (7, 256, 16, 0, "mixed"),
+                                             (13, 128, 13, 2, "mixed"), (30, 96, 30, 0, "mixed")])
 def test_slice_shell_chain_parity(gpu_lib, oracle_mod, D, n, S, K, normal):
     """One shell from the same live set, contour and key.  Every chain equals the fp32
     kernel-arithmetic oracle bit for bit (evaluation count, accepted point, log L, phantoms):
     the same RNG stream, seed choice, shrink rule and accept test in the same fp32 operation
-    order.  Against the FP64 restatement the chains agree where no likelihood comparison sits
-    within fp32 rounding of the contour (reported, not a pass criterion of the fp32 path)."""
+    order.  Priors: all Uniform, all Normal, or mixed (Normal in the odd dimensions), each
+    through the thread-per-chain kernel (D <= 16) and the warp-cooperative one.  Against the
+    FP64 restatement the chains agree where no likelihood comparison sits within fp32 rounding
+    of the contour (reported, not a pass criterion of the fp32 path)."""
     from jaxns_gb300.engine import NSBatch
     key = oracle_mod.PRNGKey(D)
     spec, (mu, cov) = _spec(D, n, S, key, seed=D, K=K)
     if normal:
-        spec.prior_kind = np.ones(D, np.int32)
-        spec.prior_a, spec.prior_b = mu + 0.2, np.full(D, 2.0)
+        kind = np.ones(D, np.int32) if normal is True else (np.arange(D) % 2).astype(np.int32)
+        spec.prior_kind = kind
+        spec.prior_a = np.where(kind == 1, mu + 0.2, -10.0)
+        spec.prior_b = np.where(kind == 1, 2.0, 20.0)
     b = NSBatch([spec])
     b.init()
     live = b.live_view(0)
