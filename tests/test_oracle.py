@@ -257,3 +257,40 @@ def test_slice_shell_margin_reports_closest_approach(oracle_mod):
     np.testing.assert_array_equal(U1, U0)
     assert np.all(np.isfinite(M1)) and np.all(M1 >= 0)
     assert np.all(M1 <= np.abs(L1 - L[99]) + 1e-12)  # the accepted point itself is one of the tests
+
+
+@pytest.mark.parametrize("guided,climb", [(True, False), (False, True)])
+def test_fp32_mode_gradient_options_both_reduction_orders(oracle_mod, guided, climb):
+    """The fp32 kernel-arithmetic mode's gradient options, in the thread kernel's sequential sums
+    and in the warp kernel's lane-butterfly sums (gradient norm, reflection dot product and
+    norm), against the FP64 restatement over a few slices at D = 40: the chains agree to fp32
+    rounding, and the two reduction orders differ only where a comparison sits within rounding
+    of the contour."""
+    from jaxns_gb300.engine import mvn_offset, mvn_params
+    D, n, S = 40, 96, 3
+    mu, cov = corr_gauss(D, D)
+    om = oracle_mod.mvn_model(-10 * np.ones(D), 10 * np.ones(D), mu, cov)
+    U = np.random.default_rng(D).uniform(0.3, 0.7, (n, D))
+    L = oracle_mod.forward(om, U)
+    o = np.argsort(L)
+    U, L = U[o], L[o]
+    s = n // 2
+    params = mvn_params(mu, cov)
+    Uo, Lo, Eo = oracle_mod.slice_shell(om, oracle_mod.PRNGKey(5), L[s - 1], U, L, s, S, gradient_guided=guided,
+                                        gradient_slice=climb)
+    outs = []
+    for warp_min_D in (17, 100):  # the warp kernel's order (variant 64), the thread kernel's (variant 0)
+        m32 = oracle_mod.model32(0, D, params, np.zeros(D, np.int32), np.full(D, -10.0), np.full(D, 20.0),
+                                 warp_min_D=warp_min_D)
+        assert m32.variant == (64 if warp_min_D == 17 else 0)
+        L32 = oracle_mod.forward32(m32, U.astype(np.float32))
+        np.testing.assert_allclose(L32.astype(np.float64) + mvn_offset(cov), L, rtol=1e-4, atol=2e-3)
+        U3, L3, E3, _, _ = oracle_mod.slice_shell32(m32, oracle_mod.PRNGKey(5), L32[s - 1], U.astype(np.float32), L32,
+                                                    s, S, gradient_guided=guided, gradient_slice=climb)
+        assert np.all(E3 >= S * 2)  # a proposal and a gradient per slice
+        same = (E3 == Eo) & np.all(np.abs(U3 - Uo) < 2e-4, axis=1)
+        assert same.mean() >= 0.9, (warp_min_D, same.mean())
+        outs.append((U3, E3))
+    (Uw, Ew), (Ut, Et) = outs
+    assert np.any(Uw.view(np.uint32) != Ut.view(np.uint32))  # the two orders round differently
+    assert np.mean((Ew == Et) & np.all(np.abs(Uw - Ut) < 2e-4, axis=1)) >= 0.9
