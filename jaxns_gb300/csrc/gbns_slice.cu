@@ -312,11 +312,18 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
   };
   grab();
 
-  // --- flattened slice / shrink loop
+  // --- flattened slice / shrink loop.  Slice starts (new direction, slice keys, chord bounds)
+  // run on every kStartCadence-th loop trip only: a lane whose slice ended waits for that trip,
+  // so the divergent start work of the warp's lanes is done together, once per kStartCadence
+  // trips.  A chain's draws and arithmetic do not depend on when its lane runs them.
+  constexpr int kStartCadence = 3;
+  int phase = 0;  // loop trips modulo kStartCadence, the same in every lane of the warp
   for (;;) {
+    const bool cadence = phase == 0;
+    phase = phase + 1 == kStartCadence ? 0 : phase + 1;
     // ---- new directions: the D normals of every lane that needs one, flattened over
     // (lane, dimension) pairs across the warp; lanes publish their keys in rank order
-    const unsigned dmask = __ballot_sync(0xffffffffu, need_dir);
+    const unsigned dmask = __ballot_sync(0xffffffffu, need_dir && cadence);
     if (dmask) {
       if (D == 1) {
         if (need_dir) d[0] = 1.0f;
@@ -351,7 +358,7 @@ __global__ void __launch_bounds__(128, GRAD ? 2 : slice_min_blocks<DMAX, FAM>())
     }
     const bool active = j < S;
     if (!__any_sync(0xffffffffu, active)) break;
-    if (!active) continue;
+    if (!active || (start && !cadence)) continue;
 
     // ---- one proposal: the first pick of slice j, or one shrink step (_new_proposal)
     Key B;
