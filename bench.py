@@ -311,8 +311,8 @@ def main():
     ap.add_argument("--warp-min-d", type=int, default=17,
                     help="correlated Gaussians with D >= this run on the warp-cooperative sampler")
     ap.add_argument("--no-adjoint", action="store_true",
-                    help="shells workload: skip the adjoint sub-record (configs[3]: one linear-regression "
-                         "problem, fused forward + adjoint against the plain GPU path + finite differences)")
+                    help="shells workload: skip the adjoint sub-record (one Bayesian linear-regression problem, "
+                         "Phi 4096 x 32: fused forward + adjoint against the plain GPU path + finite differences)")
     args = ap.parse_args()
     if args.workload in ("blr", "blr_batch"):
         return main_blr(args)
@@ -661,7 +661,7 @@ def blr_gradient_se(b, res, wl, thetas):
 
 
 def adjoint_record(h: float = 1e-3) -> dict:
-    """The metric's adjoint half on configs[3] (Bayesian linear regression, Phi 4096 x 32, 1024
+    """The metric's adjoint half on one Bayesian linear regression (Phi 4096 x 32, sigma 0.5, 1024
     live points): one problem's NS run + reweighted-evidence adjoint (log Z and
     d log Z / d(log tau, log sigma)) through the batched engine and a captured graph, timed with
     CUDA events after one warm-up, against the plain GPU path (eager launches, no graph) plus
